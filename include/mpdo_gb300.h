@@ -1,0 +1,151 @@
+/*
+ * mpdo_gb300.h -- C ABI of the GB300-native MPDO noisy-circuit engine.
+ *
+ * Plain C: opaque handles, host pointers to small parameter arrays, sizes.
+ * No torch or CUDA-runtime types appear in the signatures (streams are passed
+ * as void*).  Every call returns an mpdo_status; mpdo_last_error() gives the
+ * message of the last failing call on the calling thread.
+ *
+ * Each entry point replaces one operation of the reference's MPDO path
+ * (paths relative to the WeiguoMa/Tomography-assisted-MPDO-QCircuit root):
+ *
+ *   mpdo_chain_create      Tools.py:110-198 create_ket*Series (product state)
+ *   mpdo_apply_1q          Circuit.py:138-178 _apply_single_qubit_gate
+ *   mpdo_apply_2q          Circuit.py:74-136  _apply_two_qubits_gate
+ *   mpdo_truncate          Circuit.py:476-481 truncate layer =
+ *                          TNNOptimizer.py:72-84 bondTruncate (qr_left2right
+ *                          87-108 + svd_right2left 111-134) and
+ *                          TNNOptimizer.py:164-197 svdKappa_left2right
+ *   mpdo_kappa_truncate    TNNOptimizer.py:164-197 (the final pass of
+ *                          Circuit.py:487-489)
+ *   mpdo_reduced_dm        Circuit.py:226-295 cal_dm / _contract_dm
+ *   mpdo_probs             Tools.py:242-273 density2prob (diagonal of cal_dm)
+ *   mpdo_expect_ops        dmOperations.py:135-201 expect / pauli_expect
+ *                          (single-site operator products)
+ *   mpdo_expect_pauli_batch  many pauli_expect terms sharing one pass
+ *
+ * Layout of a site tensor in device memory: complex, row-major
+ * A[l][s][a][r] (l left bond, s physical = 2, a Kraus leg I_k, r right bond).
+ * Complex numbers crossing the ABI are interleaved (re, im) doubles.
+ */
+#ifndef MPDO_GB300_H
+#define MPDO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPDO_ABI_VERSION 1
+
+typedef enum {
+  MPDO_OK = 0,
+  MPDO_ERR_INVALID = 1,        /* bad argument (reference: ValueError) */
+  MPDO_ERR_BAD_SHAPE = 2,      /* inconsistent tensor shapes */
+  MPDO_ERR_OOM = 3,            /* device allocation failed */
+  MPDO_ERR_CUDA = 4,           /* a CUDA runtime call failed */
+  MPDO_ERR_NOT_CONVERGED = 5,  /* Jacobi hit its sweep limit (reference: LinAlgError) */
+  MPDO_ERR_NONFINITE = 6,      /* NaN/Inf met in a factorisation (reference: LinAlgError) */
+  MPDO_ERR_NO_DEVICE = 7       /* no usable CUDA device */
+} mpdo_status;
+
+typedef enum { MPDO_C64 = 0, MPDO_C128 = 1 } mpdo_dtype;
+
+typedef struct mpdo_engine_s *mpdo_engine_t;
+typedef struct mpdo_chain_s *mpdo_chain_t;
+
+int mpdo_abi_version(void);
+const char *mpdo_status_string(mpdo_status s);
+const char *mpdo_last_error(void);
+
+/* One engine per device: owns the stream, the stream-ordered memory pool and
+ * the workspaces.  Not thread-safe per handle. */
+mpdo_status mpdo_engine_create(int device, mpdo_engine_t *out);
+mpdo_status mpdo_engine_destroy(mpdo_engine_t eng);
+/* stream: a cudaStream_t, or NULL for the engine's own stream. */
+mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
+/* Engine options (no counterpart in the reference; they select between
+ * equivalent evaluation orders):
+ *   "fuse_2q"    1 (default): a 2q gate followed by truncate() is fused into
+ *                the QR sweep; 0: always split theta by SVD first (the
+ *                reference's exact sequence, including its split cutoff).
+ *   "max_sweeps" Jacobi sweep limit (default 60). */
+mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double value);
+/* Wait for all queued work; returns the first deferred device status
+ * (NOT_CONVERGED / NONFINITE) raised since the last sync. */
+mpdo_status mpdo_engine_sync(mpdo_engine_t eng);
+/* Number of kernels this engine launched so far. */
+mpdo_status mpdo_engine_launch_count(mpdo_engine_t eng, uint64_t *count);
+
+/* Product state.  vectors: n x 2 complex (4n doubles).  connected != 0 adds
+ * dimension-1 bonds between all neighbours (the reference's check_connected
+ * is then true from the start); otherwise bonds appear with the first 2q gate
+ * on each pair, as in the reference. */
+mpdo_status mpdo_chain_create(mpdo_engine_t eng, int n, int dtype, const double *vectors,
+                              int connected, mpdo_chain_t *out);
+mpdo_status mpdo_chain_destroy(mpdo_chain_t ch);
+mpdo_status mpdo_chain_clone(mpdo_chain_t src, mpdo_chain_t *out);
+mpdo_status mpdo_chain_num_sites(mpdo_chain_t ch, int *n);
+/* dims = {l, s, a, r} of one site (after any deferred work is applied). */
+mpdo_status mpdo_chain_site_dims(mpdo_chain_t ch, int site, int dims[4]);
+mpdo_status mpdo_chain_bond_present(mpdo_chain_t ch, int bond, int *present);
+/* Copy a site tensor to host: l*2*a*r complex (interleaved doubles). */
+mpdo_status mpdo_chain_read_site(mpdo_chain_t ch, int site, double *host_out);
+/* Replace a site tensor from host (dims = {l, 2, a, r}). */
+mpdo_status mpdo_chain_write_site(mpdo_chain_t ch, int site, const int dims[4],
+                                  const double *host_in);
+
+/* Gate (K = 1) or noisy gate (K Kraus operators) on one qubit.
+ * kraus: [out][in][k] complex, 2*2*K entries.  The Kraus leg is flattened
+ * into I_site after the existing one (Circuit.py:174-178). */
+mpdo_status mpdo_apply_1q(mpdo_chain_t ch, int site, const double *kraus, int K);
+
+/* Gate on the nearest-neighbour pair (site_min, site_min + 1).
+ * kraus: [o_min][o_max][i_min][i_max][k] complex, 16*K entries; the Kraus leg
+ * goes to I_{site_min+1} (Circuit.py:109-114).  abs_cutoff: the absolute
+ * singular-value cutoff of the split (GLOBAL_MINIMUM in the reference). */
+mpdo_status mpdo_apply_2q(mpdo_chain_t ch, int site_min, const double *kraus, int K,
+                          double abs_cutoff);
+
+/* truncate() layer.  chi <= 0: no bond cap; kappa <= 0: no Kraus cap;
+ * max_err < 0: no error rule; noisy != 0 runs the kappa pass.  Skipped
+ * entirely while the chain is not connected (TNNOptimizer.py:51-61).
+ * discarded_out (nullable, n-1 doubles): per-bond discarded weight
+ * sum(s_rest^2)/sum(s^2) of the SVD sweep. */
+mpdo_status mpdo_truncate(mpdo_chain_t ch, int chi, int kappa, double max_err, int noisy,
+                          double *discarded_out);
+mpdo_status mpdo_kappa_truncate(mpdo_chain_t ch, int kappa, double max_err);
+
+/* Reduced density matrix on `keep` (m ascending qubit indices; m <= 14):
+ * 2^m x 2^m complex, rows = ket (qubit keep[0] most significant). */
+mpdo_status mpdo_reduced_dm(mpdo_chain_t ch, const int *keep, int m, double *host_out);
+/* Diagonal of the reduced density matrix (real parts), 2^m doubles (m <= 24). */
+mpdo_status mpdo_probs(mpdo_chain_t ch, const int *keep, int m, double *host_out);
+/* Re Tr(rho . prod_j O_j): ops is m x (2x2 complex) [row][col], on distinct
+ * sites; identity elsewhere.  Not normalised by Tr(rho). */
+mpdo_status mpdo_expect_ops(mpdo_chain_t ch, const int *sites, const double *ops, int m,
+                            double *out);
+/* nterms Pauli strings, paulis[t*n + q] in {0:I, 1:X, 2:Y, 3:Z}; out[t] = Re Tr(rho P_t). */
+mpdo_status mpdo_expect_pauli_batch(mpdo_chain_t ch, const int8_t *paulis, int nterms,
+                                    double *out);
+
+/* Kernel-level test hooks (no counterpart in the reference).  Host in/out,
+ * row-major complex (interleaved doubles).
+ * mpdo_debug_qr:  A (m x n) = Q (m x k) R (k x n), k = min(m, n), Householder
+ *                 (TSQR for tall inputs).
+ * mpdo_debug_svd: right singular vectors of A (m x n): W (n x n, column-major,
+ *                 columns sorted by singular value, descending) and sigma (n).
+ * mpdo_debug_split: Y (m x n) ~= L (m x keep) R (keep x n), L = U_k sqrt(S_k),
+ *                 R = sqrt(S_k) V_k^H (the split used by every SVD step). */
+mpdo_status mpdo_debug_split(mpdo_engine_t eng, int dtype, int m, int n, int keep, const double *y,
+                             double *l, double *r);
+mpdo_status mpdo_debug_qr(mpdo_engine_t eng, int dtype, int m, int n, const double *a, double *q,
+                          double *r);
+mpdo_status mpdo_debug_svd(mpdo_engine_t eng, int dtype, int m, int n, const double *a, double *w,
+                           double *sigma);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPDO_GB300_H */

@@ -1,0 +1,88 @@
+"""Kernel-level GPU tests through the C-ABI test hooks: Householder QR (incl.
+TSQR levels) and QR + one-sided Jacobi SVD against numpy."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def eng():
+    mg = pytest.importorskip('mpdo_gb300')
+    if not torch.cuda.is_available():
+        pytest.skip('needs a GPU')
+    mg.build()
+    return mg.Engine.get(0)
+
+
+def _rand(m, n, seed, rank=None):
+    rng = np.random.default_rng(seed)
+    a = rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n))
+    if rank is not None:
+        u, s, vh = np.linalg.svd(a, full_matrices=False)
+        s[rank:] = 0
+        a = (u * s) @ vh
+    return a
+
+
+@pytest.mark.parametrize('m,n', [(8, 8), (40, 13), (13, 40), (512, 64), (4096, 64), (33000, 32), (300, 150)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-11), ('complex64', 5e-5)])
+def test_qr(eng, m, n, dtype, tol):
+    a = _rand(m, n, m + n)
+    q, r = eng.debug_qr(a, dtype)
+    k = min(m, n)
+    assert np.abs(q @ r - a).max() <= tol * np.abs(a).max() * 4
+    assert np.abs(q.conj().T @ q - np.eye(k)).max() <= tol * 10
+    assert np.abs(np.tril(r, -1)).max() == 0
+
+
+@pytest.mark.parametrize('m,n,rank', [(64, 64, None), (100, 20, None), (20, 100, None), (64, 64, 10), (256, 48, 5),
+                                      (16, 3, 1)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 2e-4)])
+def test_right_svd(eng, m, n, rank, dtype, tol):
+    a = _rand(m, n, 7 * m + n, rank)
+    w, s = eng.debug_svd(a, dtype)
+    s_ref = np.linalg.svd(a, compute_uv=False)
+    k = min(m, n)
+    np.testing.assert_allclose(s[:k], s_ref[:k], atol=tol * s_ref[0])
+    assert np.all(np.diff(s) <= 1e-12 * s[0] + tol * s[0])          # sorted descending
+    assert np.abs(w.conj().T @ w - np.eye(n)).max() <= tol * 10        # unitary even when rank deficient
+    # A W has orthogonal columns with norms s
+    aw = a @ w
+    g = aw.conj().T @ aw
+    np.testing.assert_allclose(np.sqrt(np.abs(np.diag(g))), s, atol=tol * 10 * s_ref[0])
+    off = g - np.diag(np.diag(g))
+    assert np.abs(off).max() <= tol * 10 * s_ref[0] ** 2
+
+
+@pytest.mark.parametrize('m,n,keep,rank', [(8, 512, 8, None), (32, 1024, 8, None), (8, 1024, 8, 3), (64, 16, 8, None),
+                                           (16, 4, 10, None), (256, 8192, 64, None), (4, 200, 6, None)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-4)])
+def test_split(eng, m, n, keep, rank, dtype, tol):
+    y = _rand(m, n, 3 * m + n, rank)
+    L, R = eng.debug_split(y, keep, dtype)
+    u, s, vh = np.linalg.svd(y, full_matrices=False)
+    k = min(keep, len(s))
+    best = (u[:, :k] * s[:k]) @ vh[:k]
+    np.testing.assert_allclose(L @ R, best, atol=tol * s[0] * 10)
+    # L = U sqrt(S): orthogonal columns with squared norms = s
+    g = L.conj().T @ L
+    np.testing.assert_allclose(np.diag(g).real[:k], s[:k], rtol=tol * 10, atol=tol * s[0])
+    if keep > k:
+        assert np.abs(L[:, k:]).max() == 0 and np.abs(R[k:]).max() == 0
+
+
+@pytest.mark.parametrize('dtype,scale,tol', [('complex128', 1e-160, 1e-11), ('complex64', 1e-21, 5e-5)])
+def test_qr_columns_near_underflow(eng, dtype, scale, tol):
+    # rank-deficient factors carry junk directions whose squares underflow;
+    # the reflectors must stay unitary (scaled norms)
+    a = _rand(128, 64, 5)
+    a[:, 40:] *= scale
+    a[60:, 48:] = 0
+    q, r = eng.debug_qr(a, dtype)
+    assert np.isfinite(q).all() and np.isfinite(r).all()
+    assert np.abs(q.conj().T @ q - np.eye(64)).max() <= tol * 10
+    assert np.abs(q @ r - a).max() <= tol * np.abs(a).max() * 4
+    w, s = eng.debug_svd(a, dtype)
+    assert np.isfinite(w).all() and np.abs(w.conj().T @ w - np.eye(64)).max() <= tol * 10

@@ -1,0 +1,290 @@
+"""TensorCircuit: the reference's MPDO simulator API over the GB300 engine
+(reference: MPDOSimulator/Circuit.py).
+
+``evolve`` walks the queued layers exactly as the reference does
+(Circuit.py:469-491): gates are contracted into the MPDO sites, ``truncate()``
+layers run the QR left-to-right / SVD right-to-left bond sweep and then the
+kappa SVD pass (only once the chain is connected), and a final kappa pass
+follows when the last layer is not a truncate.  Every contraction and
+factorisation runs on the GPU through ``libmpdo_gb300.so``; there is no CPU
+path.
+"""
+import math
+from typing import Any, Dict, List, Optional, Tuple, Union
+
+import numpy as np
+import torch
+from torch.linalg import LinAlgError
+
+from .AbstractCircuit import QuantumCircuit
+from .NoiseChannel import NoiseChannel
+from .QuantumGates.AbstractGate import QuantumGate
+from .QuantumGates.SingleGates import MeasureX, MeasureY
+from .Tools import QubitNode, count_item
+from . import dmOperations
+
+GLOBAL_MINIMUM = 2.718281828459045 * 1e-8       # Circuit.py:22
+MAX_ATTEMPTS = 4                                 # Circuit.py:23
+
+
+def _cuda_index(device) -> int:
+    if isinstance(device, int):
+        return device
+    if isinstance(device, str) and device.startswith('cuda'):
+        return int(device.split(':')[1]) if ':' in device else 0
+    return 0
+
+
+class TensorCircuit(QuantumCircuit):
+    def __init__(self, qn: int, ideal: bool = True, noiseType: str = 'no',
+                 chiFileDict: Optional[Dict[str, Dict[str, Any]]] = None,
+                 chi: Optional[int] = None, kappa: Optional[int] = None,
+                 max_truncation_err: Optional[float] = None, chip: Optional[str] = None,
+                 dtype=torch.complex64, device: Optional[Union[str, int]] = None):
+        """Circuit.py:27-63.  ``device`` selects where returned tensors live; the
+        evolution itself always runs on a CUDA device (``cuda:k`` picks which)."""
+        super().__init__(noiseFiles=chiFileDict, chi=chi, kappa=kappa, max_truncation_err=max_truncation_err,
+                         dtype=dtype, device=device)
+        if dtype not in (torch.complex64, torch.complex128):
+            raise ValueError('dtype must be torch.complex64 or torch.complex128')
+        self.qnumber = qn
+        self.ideal = ideal
+        self.noiseType = noiseType.lower()
+        self.Noise = None
+        self._chain = None
+        self.discarded_weights: List[np.ndarray] = []
+        if not ideal:
+            if self.noiseType not in ['unified', 'realnoise', 'idealnoise']:
+                raise ValueError(f'Unsupported noise type: {self.noiseType}')
+            self.Noise = NoiseChannel(chip=chip, dtype=dtype, device=self.device)
+            self.unified = self.noiseType == 'unified'
+            self.realNoise = self.noiseType == 'realnoise'
+            self.idealNoise = self.noiseType == 'idealnoise'
+            if self.realNoise:
+                self._load_exp_tensors()
+
+    # ---------------------------------------------------------- engine ---
+    def _engine(self):
+        from mpdo_gb300 import Engine
+        return Engine.get(_cuda_index(self.device))
+
+    @staticmethod
+    def _np(t) -> np.ndarray:
+        return t.detach().to('cpu', torch.complex128).numpy()
+
+    def _noisy_1q(self, gate: QuantumGate) -> np.ndarray:
+        """Circuit.py:141-155 (composite cached per name for fixed gates)."""
+        g = gate.tensor
+        if not ((self.idealNoise or self.unified) and not gate.ideal):
+            return self._np(g)
+        key = None if (gate.variational or gate.name == 'ArbSingleGate') else gate.name
+        if key is not None and key in self.noiseTensorDict:
+            return self.noiseTensorDict[key]
+        t = torch.einsum('nlm, ljk, ji -> nimk', self.Noise.decayTensor.to(g.device),
+                         self.Noise.dephasingTensor.to(g.device), g.to(self.Noise.decayTensor.dtype))
+        t = self._np(t.reshape(2, 2, -1))
+        if key is not None:
+            self.noiseTensorDict[key] = t
+        return t
+
+    def _noisy_2q(self, gate: QuantumGate) -> np.ndarray:
+        """Circuit.py:84-100: idealNoise appends 2q depolarising after the gate;
+        realNoise gates (CZEXP/CPEXP) carry their own Kraus leg."""
+        g = gate.tensor
+        gnoise = (self.idealNoise and not gate.ideal) or self.realNoise
+        if not gnoise or self.realNoise:
+            return self._np(g)
+        key = None if gate.variational else '2q:' + gate.name
+        if key is not None and key in self.noiseTensorDict:
+            return self.noiseTensorDict[key]
+        t = self._np(torch.einsum('ijklp, klmn -> ijmnp', self.Noise.dpCTensor2.to(g.device),
+                                  g.to(self.Noise.dpCTensor2.dtype)))
+        if key is not None:
+            self.noiseTensorDict[key] = t
+        return t
+
+    def _add_gate(self, chain, _layer_num: int, _oqs: List[int], _gate: Optional[QuantumGate] = None):
+        """Circuit.py:180-224."""
+        if not isinstance(_oqs, list):
+            raise TypeError('Operating qubits must be a list.')
+        if _oqs[0] is None:
+            return None
+        if max(_oqs) >= self.qnumber:
+            raise ValueError(f'Qubit index out of range, max index is Q{max(_oqs)}.')
+        gate = _gate or self.layers[_layer_num]
+        if not gate or gate.name == 'MeasureZ':
+            return None
+        if not isinstance(gate, QuantumGate):
+            raise TypeError(f'Gate must be a QuantumGate, current type is {type(gate)}.')
+        if gate.single:
+            t = self._noisy_1q(gate)
+            for q in _oqs:
+                chain.apply_1q(q, t)
+        else:
+            if len(_oqs) != 2 or _oqs[0] == _oqs[1]:
+                raise ValueError('Invalid operating qubits for a two-qubit gate.')
+            a, b = _oqs
+            if abs(a - b) != 1:
+                raise ValueError('Only nearest-neighbour two-qubit gates are supported by the MPDO engine.')
+            t = self._noisy_2q(gate)
+            if t.ndim == 4:
+                t = t[..., None]
+            if a > b:
+                t = np.transpose(t, (1, 0, 3, 2, 4))
+            chain.apply_2q(min(a, b), t, GLOBAL_MINIMUM)
+
+    def evolve(self, state: List[QubitNode]):
+        """Circuit.py:469-491."""
+        from mpdo_gb300 import Chain
+        if len(state) != self.qnumber:
+            raise ValueError('state length differs from the number of qubits')
+        self._initState = [QubitNode(s.tensor.clone(), s.name, s.axis_names, s.connected) for s in state]
+        vectors = np.stack([self._np(s.tensor).reshape(2) for s in state])
+        connected = all(getattr(s, 'connected', False) for s in state)
+        dt = 'complex128' if self.dtype == torch.complex128 else 'complex64'
+        chain = Chain(vectors, dtype=dt, connected=connected, engine=self._engine())
+        noisy = not self.ideal
+        self.discarded_weights = []
+        last = None
+        for i, layer in enumerate(self.layers):
+            name = layer.name.lower()
+            if 'truncate' in name:
+                d = chain.truncate(self.chi, self.kappa, self.max_truncation_err, noisy, report=True)
+                self.discarded_weights.append(d)
+            elif 'barrier' in name:
+                pass
+            else:
+                self._add_gate(chain, i, self._oqs_list[i])
+            last = name
+        if noisy and last is not None and 'truncate' not in last:          # Circuit.py:487-489
+            chain.kappa_truncate(self.kappa, self.max_truncation_err)
+        self._chain = chain
+        self._dm, self._dmNodes, self._vector = None, None, None
+        nodes = [QubitNode(None, f'qubit_{k}', [f'bond_{k - 1}_{k}', f'physics_{k}', f'I_{k}', f'bond_{k}_{k + 1}'],
+                           chain=chain, index=k, dtype=self.dtype, device=self.device) for k in range(self.qnumber)]
+        self._stateNodes = nodes
+        state[:] = nodes
+        return nodes
+
+    def forward(self, state):
+        self.evolve(state)
+
+    def _need_chain(self):
+        if self._chain is None:
+            raise RuntimeError('evolve(state) first')
+        return self._chain
+
+    # --------------------------------------------------------- readout ---
+    def cal_vector(self):
+        """Circuit.py:264-272 (ideal circuits only)."""
+        if not self.ideal:
+            raise ValueError('Noisy circuit cannot be represented by state vector efficiently.')
+        ch = self._need_chain()
+        psi = np.ones((1, 1), dtype=np.complex128)
+        for k in range(self.qnumber):
+            a = ch.site(k)                                        # (l, 2, 1, r)
+            psi = np.einsum('pl,lsr->psr', psi, a[:, :, 0, :]).reshape(-1, a.shape[3])
+        v = torch.as_tensor(psi.reshape(2 ** self.qnumber, 1)).to(dtype=self.dtype, device=self.device)
+        self._vector = v
+        return v
+
+    def cal_dmNodes(self, reduced_index: Optional[List] = None):
+        """Circuit.py:274-280: a handle on the doubled network (ket + conj)."""
+        nodes = dmOperations.DMNodes(self._need_chain(), self.qnumber, self.dtype, self.device)
+        if reduced_index:
+            nodes.trace_out(reduced_index)
+        self._dmNodes = nodes
+        return nodes
+
+    def cal_dm(self, reduced_index: Optional[List] = None, _replicate_require: bool = False):
+        """Circuit.py:282-295: rho (or the reduced rho with ``reduced_index``
+        traced out), rows = ket legs, qubit order ascending."""
+        reduced_index = [] if reduced_index is None else list(reduced_index)
+        if reduced_index and max(reduced_index) >= self.qnumber:
+            raise ValueError('Reduced index should not be larger than the qubit number.')
+        keep = [q for q in range(self.qnumber) if q not in reduced_index]
+        rho = self._need_chain().reduced_dm(keep)
+        self._dm = torch.as_tensor(rho).to(dtype=self.dtype, device=self.device)
+        return self._dm
+
+    def probabilities(self, keep: Optional[List[int]] = None) -> torch.Tensor:
+        """Diagonal of the (reduced) density matrix without forming it."""
+        p = self._need_chain().probs(keep)
+        return torch.as_tensor(p)
+
+    # -------------------------------------------------------- sampling ---
+    def _conditional_prb(self, chain, order: List[int], history: List[int]) -> float:
+        """Circuit.py:297-332: p(1 | history) on qubit order[len(history)],
+        the other unmeasured qubits traced, GLOBAL_MINIMUM added to both."""
+        q = order[len(history)]
+        proj = [np.diag([1.0, 0.0]).astype(np.complex128), np.diag([0.0, 1.0]).astype(np.complex128)]
+        ops = {order[j]: proj[h] for j, h in enumerate(history)}
+        p = []
+        for v in (0, 1):
+            o = dict(ops)
+            o[q] = proj[v]
+            p.append(chain.expect_ops(o) + GLOBAL_MINIMUM)
+        p = np.asarray(p)
+        if (p < 0).any():
+            raise RuntimeError(f'State is illegal, and your probability distribution is {p}.')
+        return float(p[1] / p.sum())
+
+    def sample(self, shots: Optional[int] = None, orientation: Optional[List[int]] = None,
+               reduced: Optional[List[int]] = None, sample_string: bool = True, _tqdm_disable: bool = False,
+               _require_sequential_sample: bool = False, _require_bool_result: bool = False,
+               _require_counts: bool = True, _stateNodes4Sample=None):
+        """Circuit.py:389-446 (batch conditional sampling, 344-387)."""
+        shots = shots or 1024
+        reduced = reduced or []
+        order = [q for q in range(self.qnumber) if q not in reduced]
+        L = len(order)
+        orientation = orientation or [2] * L
+        if len(orientation) != L:
+            raise ValueError('Length of orientation must match the sample length. Check reduced or unmeasured qubits.')
+        chain = self._need_chain().clone()
+        for val, M in [(0, MeasureX), (1, MeasureY)]:
+            idx = [order[i] for i, v in enumerate(orientation) if v == val]
+            if idx:
+                g = self._np(M(dtype=self.dtype, device='cpu').tensor)
+                for q in idx:
+                    chain.apply_1q(q, g)
+        seq = torch.zeros((shots, L), dtype=torch.bool if _require_bool_result else torch.int)
+        one = True if _require_bool_result else 1
+        groups = [self.Group(history=[], start=0, length=shots)]
+        for pos in range(L):
+            new = []
+            for grp in groups:
+                if grp.length == 0:
+                    continue
+                p1 = self._conditional_prb(chain, order, grp.history)
+                if p1 < GLOBAL_MINIMUM:
+                    k1 = 0
+                elif p1 > 1 - GLOBAL_MINIMUM:
+                    k1 = grp.length
+                else:
+                    k1 = int(torch.bernoulli(torch.full((grp.length,), p1)).sum())
+                k0 = grp.length - k1
+                seq[grp.start: grp.start + k1, pos] = one
+                if pos < L - 1:
+                    if k1 > 0:
+                        new.append(self.Group(grp.history + [1], grp.start, k1))
+                    if k0 > 0:
+                        new.append(self.Group(grp.history + [0], grp.start + k1, k0))
+            groups = new
+        bits = seq.tolist()
+        if sample_string and not _require_bool_result:
+            bits = [''.join(map(str, b)) for b in bits]
+        self._samples = bits
+        if _require_counts:
+            self._counts = count_item(bits)
+            return self._samples, self._counts
+        return self._samples
+
+    def randomSample(self, measurement_schemes: List[List[int]], shots_per_scheme: int = 1024,
+                     reduced: Optional[List[int]] = None, _tqdm_disable: bool = False,
+                     _require_sequential_sample: bool = False, _require_bool_result: bool = False,
+                     _stateNodes4Sample=None):
+        """Circuit.py:448-466."""
+        return [self.sample(shots=shots_per_scheme, orientation=s, reduced=reduced, sample_string=False,
+                            _tqdm_disable=True, _require_bool_result=_require_bool_result, _require_counts=False)
+                for s in measurement_schemes]

@@ -1,0 +1,181 @@
+"""Gate base classes (reference: QuantumGates/AbstractGate.py:13-99).
+
+Gate tensors are built with differentiable torch ops (the reference rebuilds
+them through ``torch.tensor(data=...)``, which detaches the angle from the
+graph); index order is [out, in] for one qubit and [out0, out1, in0, in1] for
+two qubits, as in the reference.
+"""
+from abc import ABC, abstractmethod
+from typing import Optional
+
+import torch
+from torch import Tensor, nn
+
+
+class Truncate(nn.Module):
+    def __init__(self):
+        super().__init__()
+        self.name = 'truncate'
+
+    def forward(self, *args, **kwargs):
+        pass
+
+
+class Barrier(nn.Module):
+    def __init__(self):
+        super().__init__()
+        self.name = 'barrier'
+
+    def forward(self, *args, **kwargs):
+        pass
+
+
+class QuantumGate(ABC, nn.Module):
+    """Base class for quantum gates (AbstractGate.py:31-99)."""
+
+    def __init__(self, ideal: Optional[bool] = True, dtype=torch.complex64, device='cpu'):
+        super().__init__()
+        self.para = None
+        self._ideal = ideal
+        self.dtype, self.device = dtype, device
+
+    def _check_Para_Tensor(self, *parameters):
+        def conv(p):
+            if isinstance(p, Tensor):
+                return p.to(device=self.device)
+            if isinstance(p, (float, int)):
+                return torch.tensor(float(p), dtype=torch.float64, device=self.device)
+            raise ValueError(f'Invalid type for gate parameter: {type(p)}')
+        ps = [conv(p) for p in parameters]
+        return ps if len(parameters) > 1 else ps[0]
+
+    def _mat(self, rows):
+        """Stack a nested list of (possibly tensor-valued) entries into a complex
+        matrix, keeping autograd through tensor entries."""
+        cdt = self.dtype
+        out = []
+        for row in rows:
+            out.append(torch.stack([torch.as_tensor(x, device=self.device).to(cdt) for x in row]))
+        return torch.stack(out)
+
+    @property
+    @abstractmethod
+    def name(self):
+        pass
+
+    @property
+    @abstractmethod
+    def tensor(self):
+        pass
+
+    @property
+    @abstractmethod
+    def rank(self):
+        pass
+
+    @property
+    @abstractmethod
+    def dimension(self):
+        pass
+
+    @property
+    @abstractmethod
+    def single(self) -> bool:
+        pass
+
+    @property
+    @abstractmethod
+    def variational(self) -> bool:
+        pass
+
+    @property
+    def para(self):
+        return self._para
+
+    @para.setter
+    def para(self, para):
+        self._para = para
+
+    @property
+    def ideal(self) -> Optional[bool]:
+        return self._ideal
+
+    @ideal.setter
+    def ideal(self, value: Optional[bool]):
+        if not isinstance(value, bool):
+            raise ValueError('Value must be bool.')
+        self._ideal = value
+
+
+def _cexp(x):
+    """exp(1j * x) for a real tensor/float, differentiable."""
+    x = torch.as_tensor(x, dtype=torch.float64) if not isinstance(x, Tensor) else x
+    if x.is_complex():
+        return torch.exp(1j * x)
+    return torch.complex(torch.cos(x), torch.sin(x))
+
+
+class _Fixed(QuantumGate):
+    """A constant gate defined by a matrix literal."""
+    _NAME = ''
+    _DATA = None
+    _SINGLE = True
+
+    def __init__(self, ideal: Optional[bool] = None, dtype=torch.complex64, device='cpu'):
+        super().__init__(ideal=ideal, dtype=dtype, device=device)
+
+    @property
+    def name(self):
+        return self._NAME
+
+    @property
+    def tensor(self):
+        t = torch.tensor(self._DATA, dtype=self.dtype, device=self.device)
+        return t if self._SINGLE else t.reshape(2, 2, 2, 2)
+
+    @property
+    def rank(self):
+        return 2 if self._SINGLE else 4
+
+    @property
+    def dimension(self):
+        return [2, 2] if self._SINGLE else [[2, 2], [2, 2]]
+
+    @property
+    def single(self) -> bool:
+        return self._SINGLE
+
+    @property
+    def variational(self) -> bool:
+        return False
+
+
+class _Param(QuantumGate):
+    """A parameterised gate; subclasses define ``_build()``."""
+    _NAME = ''
+    _SINGLE = True
+
+    @property
+    def name(self):
+        return self._NAME
+
+    @property
+    def rank(self):
+        return 2 if self._SINGLE else 4
+
+    @property
+    def dimension(self):
+        return [2, 2] if self._SINGLE else [[2, 2], [2, 2]]
+
+    @property
+    def single(self) -> bool:
+        return self._SINGLE
+
+    @property
+    def variational(self) -> bool:
+        return True
+
+    @property
+    def tensor(self):
+        t = self._build()
+        return t if self._SINGLE else t.reshape(2, 2, 2, 2)

@@ -1,0 +1,1126 @@
+// MPDO engine: chain state on the device, the hot-path operations and the
+// C ABI declared in include/mpdo_gb300.h.
+//
+// Reference operations restated here (paths relative to the reference root):
+//   Circuit.py:138-178  single-qubit (noisy) gate         -> apply_1q
+//   Circuit.py:74-136   two-qubit gate + SVD split         -> apply_2q / materialize_pair
+//   TNNOptimizer.py:87-108  qr_left2right                  -> qr_sweep
+//   TNNOptimizer.py:111-134 svd_right2left                 -> svd_sweep
+//   TNNOptimizer.py:164-197 svdKappa_left2right            -> kappa_pass
+//   Circuit.py:226-295, dmOperations.py:135-201 readout    -> env_* / reduced_dm / expect
+//
+// Deferred two-qubit gates.  A 2q gate is recorded on its pair and applied
+// lazily.  If the next operation touching the pair is a truncate() that runs,
+// the gate is fused into the QR left-to-right sweep: the reference would split
+// theta by an SVD (Circuit.py:116-126) and immediately re-orthogonalise the
+// left factor by QR (TNNOptimizer.py:98-106), which leaves the state equal to
+// theta up to the split's cutoff (tail weight below GLOBAL_MINIMUM-level).
+// The fused step factors the left site directly by Householder QR and pushes
+// the gate into the right site, so no SVD of theta is needed.  Any other
+// operation on the pair (another gate, readout, a skipped truncate followed
+// by readout) materialises the gate with the reference's SVD split and its
+// cutoff rule.
+#include "kernels.cuh"
+#include "mpdo_gb300.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace mpdo {
+
+// ------------------------------------------------------------ errors ----
+struct Error {
+  mpdo_status st;
+  std::string msg;
+};
+[[noreturn]] static void fail(mpdo_status s, const std::string &m) { throw Error{s, m}; }
+
+static thread_local std::string g_last_error;
+
+// ------------------------------------------------------------ engine ----
+struct Engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  cudaMemPool_t pool = nullptr;
+  int *d_status = nullptr;
+  int status_cap = 8192;
+  int status_used = 0;
+  bool fuse_2q = true;
+  int max_sweeps = 60;
+  int first_status = 0;
+};
+
+static void *dalloc(Engine &e, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  void *p = nullptr;
+  cudaError_t err = cudaMallocFromPoolAsync(&p, bytes, e.pool, e.stream);
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    fail(MPDO_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(err));
+  }
+  return p;
+}
+static void dfree(Engine &e, void *p) {
+  if (p) MPDO_CUDA_CHECK(cudaFreeAsync(p, e.stream));
+}
+
+// Scoped device buffer
+template <typename X> struct DBuf {
+  Engine *e = nullptr;
+  X *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(Engine &eng, size_t count) : e(&eng), n(count) { p = static_cast<X *>(dalloc(eng, count * sizeof(X))); }
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : e(o.e), p(o.p), n(o.n) { o.p = nullptr; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    reset();
+    e = o.e; p = o.p; n = o.n; o.p = nullptr;
+    return *this;
+  }
+  X *release() { X *q = p; p = nullptr; return q; }
+  void reset() { if (p && e) dfree(*e, p); p = nullptr; }
+  ~DBuf() { if (p && e) { cudaFreeAsync(p, e->stream); } }
+};
+
+static int *status_slot(Engine &e, int count);
+static void check_status(Engine &e);
+
+// ------------------------------------------------------------- chain ----
+struct Site {
+  void *p = nullptr;
+  int l = 1, a = 1, r = 1;
+  size_t elems() const { return (size_t)l * 2 * a * r; }
+};
+struct Pend {
+  bool on = false;
+  std::vector<double> t;
+  int K = 1;
+  double cutoff = 0;
+};
+}  // namespace mpdo
+
+struct mpdo_engine_s {
+  mpdo::Engine e;
+};
+struct mpdo_chain_s {
+  mpdo_engine_s *eng = nullptr;
+  int n = 0;
+  int dtype = MPDO_C64;
+  std::vector<mpdo::Site> s;
+  std::vector<char> bond;
+  std::vector<mpdo::Pend> pend;
+};
+
+namespace mpdo {
+
+// ---------------------------------------------------------- helpers -----
+template <typename T> static View<T> RM(const cx<T> *p, int64_t ld, int conj = 0, int64_t bs = 0) {
+  return View<T>{p, bs, 1, ld, 0, 1, conj};
+}
+template <typename T> static View<T> CM(const cx<T> *p, int64_t ld, int conj = 0, int64_t bs = 0) {
+  return View<T>{p, bs, 1, 1, 0, ld, conj};
+}
+
+template <typename T>
+static void gemm(Engine &e, int M, int N, int K, const View<T> &A, const View<T> &B, cx<T> *C, int64_t ldc,
+                 int batch = 1, int64_t cbs = 0, cx<T> beta = czero<T>()) {
+  // split-K workspace for small-output long-K products (Gram matrices)
+  const int64_t tiles = (int64_t)((M + 63) / 64) * ((N + 63) / 64) * batch;
+  if (K >= 512 && tiles < 148) {
+    const int nsplit = (int)std::min<int64_t>(std::max<int64_t>(1, 296 / tiles), K / 128);
+    if (nsplit > 1) {
+      const size_t ws = (size_t)nsplit * batch * M * N;
+      DBuf<cx<T>> w(e, ws);
+      cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs, w.p, ws);
+      return;
+    }
+  }
+  cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs);
+}
+
+template <typename T> static cx<T> *site_ptr(mpdo_chain_s *ch, int i) { return static_cast<cx<T> *>(ch->s[i].p); }
+
+template <typename T> static void set_site(mpdo_chain_s *ch, int i, cx<T> *p, int l, int a, int r) {
+  Engine &e = ch->eng->e;
+  if (ch->s[i].p) dfree(e, ch->s[i].p);
+  ch->s[i].p = p;
+  ch->s[i].l = l; ch->s[i].a = a; ch->s[i].r = r;
+}
+
+// ---------------------------------------------------------------- QR ----
+// Householder QR of an m x n matrix (view `in`): Q (m x k, row-major, ld k),
+// R (k x n row-major), k = min(m, n).  Tall-skinny inputs go through TSQR
+// levels of shared-memory-resident chunks.
+template <typename T>
+static void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
+  const size_t esz = sizeof(cx<T>);
+  const size_t cap = 200 * 1024;
+  struct Level {
+    int m, mc, nch;
+    DBuf<cx<T>> v, tau, rs;
+  };
+  std::vector<Level> lv;
+  View<T> cur = in;
+  int curm = m;
+  while (true) {
+    int mc;
+    if ((size_t)curm * n * esz <= cap) mc = curm;
+    else if (n <= 128 && (size_t)curm >= 4 * (size_t)n) {
+      size_t mcs = cap / ((size_t)(n + 1) * esz);
+      mcs = mcs / 32 * 32;
+      if (mcs < 2 * (size_t)n) mc = curm; else mc = (int)std::min<size_t>(mcs, (size_t)curm);
+    } else mc = curm;
+    const int nch = (curm + mc - 1) / mc;
+    Level L;
+    L.m = curm; L.mc = mc; L.nch = nch;
+    L.v = DBuf<cx<T>>(e, (size_t)nch * mc * n);
+    L.tau = DBuf<cx<T>>(e, (size_t)nch * n);
+    L.rs = DBuf<cx<T>>(e, (size_t)nch * n * n);
+    qr_factor_chunks<T>(e.stream, curm, n, mc, nch, cur, L.v.p, L.tau.p, L.rs.p);
+    lv.push_back(std::move(L));
+    if (nch == 1) break;
+    cur = RM<T>(lv.back().rs.p, n);
+    curm = nch * n;
+  }
+  const int k = std::min(m, n);
+  const Level &top = lv.back();
+  const int ktop = std::min(top.m, n);
+  if (ktop != k) fail(MPDO_ERR_BAD_SHAPE, "internal TSQR rank mismatch");
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(R, top.rs.p, (size_t)k * n * esz, cudaMemcpyDeviceToDevice, e.stream));
+  if (Q == nullptr) return;
+  // Q top-down
+  DBuf<cx<T>> qa, qb;
+  const cx<T> *bin = nullptr;
+  for (int li = (int)lv.size() - 1; li >= 0; --li) {
+    const Level &L = lv[li];
+    cx<T> *out;
+    if (li == 0) out = Q;
+    else {
+      DBuf<cx<T>> nb(e, (size_t)L.m * k);
+      out = nb.p;
+      if (li % 2) { qa = std::move(nb); } else { qb = std::move(nb); }
+    }
+    qr_apply_chunks<T>(e.stream, L.m, n, L.mc, L.nch, L.v.p, L.tau.p, bin, k, k, out, k);
+    bin = out;
+  }
+}
+
+// ------------------------------------------------------------ SVD -----
+// Right singular vectors of an m x n matrix given by a view: Householder QR
+// (R is k x n, k = min(m, n)), then one-sided Jacobi on the columns of R with
+// the rotations accumulated: R W = U diag(sigma).  W (n x n, column-major,
+// columns sorted by sigma descending) is unitary to rounding whatever the
+// rank; sigma has n entries (zeros beyond the rank).
+template <typename T>
+static void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W, DBuf<T> &sigma) {
+  const int k = std::min(m, n);
+  DBuf<cx<T>> R(e, (size_t)k * n);
+  qr<T>(e, m, n, in, nullptr, R.p);
+  W = DBuf<cx<T>>(e, (size_t)n * n);
+  sigma = DBuf<T>(e, n);
+  DBuf<cx<T>> U(e, (size_t)k * n), xws(e, (size_t)k * n), wws(e, (size_t)n * n);
+  jacobi_svd<T>(e.stream, 1, k, n, RM<T>(R.p, n), U.p, sigma.p, W.p, xws.p, wws.p, e.max_sweeps,
+                status_slot(e, 1));
+}
+
+// --------------------------------------------------------- SVD split ----
+// Y (Mr x Nc, row-major) = L R with L = U_k sqrt(S_k) (Mr x keep, ld keep)
+// and R = sqrt(S_k) V_k^H (keep x Nc), keep chosen by keep_fn(s_dev, nsv).
+// The left singular vectors of Y are the right singular vectors of Y^H:
+// QR of Y^H, one-sided Jacobi on R.  R_out is formed as s^-1/2 U_k^H Y.
+// When keep exceeds min(Mr, Nc) the extra columns/rows are zero (the
+// reference's SVD returns (near-)zero singular values there).
+// wsum (nullable): device double[2] = {kept, total} sum s^2.
+template <typename T, typename KeepFn>
+static void svd_split(Engine &e, const cx<T> *Y, int Mr, int Nc, KeepFn keep_fn, DBuf<cx<T>> &Lout,
+                      DBuf<cx<T>> &Rout, int &keep_out, double *wsum) {
+  DBuf<cx<T>> W;
+  DBuf<T> sg;
+  right_svd<T>(e, Nc, Mr, CM<T>(Y, Nc, 1), W, sg);       // view of Y^H (Nc x Mr)
+  const int nsv_ref = std::min(Mr, Nc);
+  const int keep = keep_fn(sg.p, nsv_ref);
+  keep_out = keep;
+  if (wsum) sigma_weights<T>(e.stream, sg.p, Mr, keep, wsum);
+  const int kk = std::min(keep, nsv_ref);
+  Lout = DBuf<cx<T>>(e, (size_t)Mr * std::max(keep, 1));
+  Rout = DBuf<cx<T>>(e, (size_t)std::max(keep, 1) * Nc);
+  if (keep > kk) {
+    fill_zero<T>(e.stream, Lout.p, (size_t)Mr * keep);
+    fill_zero<T>(e.stream, Rout.p, (size_t)keep * Nc);
+  }
+  if (kk <= 0) return;
+  // L = W[:, :kk] sqrt(s)  (W column-major: element (i, j) at j*Mr + i)
+  {
+    const int64_t d[4] = {1, 1, Mr, kk};
+    const int64_t st[4] = {0, 0, 1, Mr};
+    if (keep == kk) {
+      copy4d<T>(e.stream, Lout.p, W.p, d, st, 0);
+    } else {
+      DBuf<cx<T>> Lk(e, (size_t)Mr * kk);
+      copy4d<T>(e.stream, Lk.p, W.p, d, st, 0);
+      MPDO_CUDA_CHECK(cudaMemcpy2DAsync(Lout.p, keep * sizeof(cx<T>), Lk.p, kk * sizeof(cx<T>), kk * sizeof(cx<T>),
+                                        Mr, cudaMemcpyDeviceToDevice, e.stream));
+    }
+  }
+  scale_matrix<T>(e.stream, Lout.p, Mr, kk, keep, sg.p, 0, 1);
+  // R = s^-1/2 W[:, :kk]^H Y
+  gemm<T>(e, kk, Nc, Mr, RM<T>(W.p, Mr, 1), RM<T>(Y, Nc), Rout.p, Nc);
+  scale_matrix<T>(e.stream, Rout.p, kk, Nc, Nc, sg.p, 1, 2);
+}
+
+// decompositions.py:121-134 truncation rule on host singular values.  The
+// reference decomposes a matrix with nsv singular values; entries beyond the
+// computed spectrum are zero.
+template <typename T>
+static int error_rule_keep(const std::vector<T> &s_in, int nsv, int max_sv, double err, bool relative) {
+  int n_err = max_sv;
+  if (err >= 0 && nsv > 0) {
+    std::vector<T> te(nsv);
+    T acc = T(0);
+    for (int i = 0; i < nsv; ++i) {
+      const T v = i < (int)s_in.size() ? s_in[i] : T(0);
+      acc += v * v;
+      te[i] = std::sqrt(acc);
+    }
+    const T s0 = s_in.empty() ? T(0) : s_in[0];
+    const T thr = relative ? (T)err * s0 : (T)err;
+    for (int idx = 0; idx < nsv - 1; ++idx)
+      if (te[nsv - 1] - te[idx] <= thr) { n_err = idx + 1; break; }
+  }
+  return std::min(max_sv, n_err);
+}
+
+// -------------------------------------------------------------- ops -----
+template <typename T> static void materialize_pair(mpdo_chain_s *ch, int i);
+
+template <typename T> static void materialize_touching(mpdo_chain_s *ch, int site) {
+  if (site - 1 >= 0 && ch->pend[site - 1].on) materialize_pair<T>(ch, site - 1);
+  if (site < ch->n - 1 && ch->pend[site].on) materialize_pair<T>(ch, site);
+}
+template <typename T> static void materialize_all(mpdo_chain_s *ch) {
+  for (int i = 0; i + 1 < ch->n; ++i)
+    if (ch->pend[i].on) materialize_pair<T>(ch, i);
+}
+
+template <typename T> static void apply_1q(mpdo_chain_s *ch, int site, const double *kraus, int K) {
+  Engine &e = ch->eng->e;
+  materialize_touching<T>(ch, site);
+  const Site s = ch->s[site];
+  DBuf<cx<T>> out(e, (size_t)s.l * 2 * s.a * K * s.r);
+  kraus1q<T>(e.stream, site_ptr<T>(ch, site), out.p, s.l, s.a, s.r, kraus, K);
+  set_site<T>(ch, site, out.release(), s.l, s.a * K, s.r);
+}
+
+template <typename T> static void materialize_pair(mpdo_chain_s *ch, int i) {
+  Engine &e = ch->eng->e;
+  Pend pd = ch->pend[i];
+  ch->pend[i].on = false;
+  const Site A = ch->s[i], B = ch->s[i + 1];
+  const int l = A.l, a = A.a, m = A.r, c = B.a, r = B.r, K = pd.K;
+  const int Mr = l * 2 * a, Nc = 2 * c * K * r;
+  DBuf<cx<T>> P(e, (size_t)Mr * 2 * c * r);
+  gemm<T>(e, Mr, 2 * c * r, m, RM<T>(site_ptr<T>(ch, i), m), RM<T>(site_ptr<T>(ch, i + 1), 2 * c * r), P.p,
+          2 * c * r);
+  DBuf<cx<T>> th(e, (size_t)Mr * Nc);
+  mix2q_batched<T>(e.stream, P.p, th.p, l, a, c, r, pd.t.data(), K);
+  P.reset();
+  // Circuit.py:116-126: exact SVD, absolute cutoff, no cap
+  const double cutoff = pd.cutoff;
+  auto keep_fn = [&](const T *s_dev, int nsv) -> int {
+    std::vector<T> s(std::min(Mr, Nc));
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(s.data(), s_dev, s.size() * sizeof(T), cudaMemcpyDeviceToHost, e.stream));
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+    return error_rule_keep<T>(s, nsv, nsv, cutoff, false);
+  };
+  DBuf<cx<T>> Lf, Rf;
+  int keep = 0;
+  svd_split<T>(e, th.p, Mr, Nc, keep_fn, Lf, Rf, keep, nullptr);
+  set_site<T>(ch, i, Lf.release(), l, a, keep);
+  set_site<T>(ch, i + 1, Rf.release(), keep, c * K, r);
+}
+
+template <typename T> static void apply_2q(mpdo_chain_s *ch, int i, const double *t, int K, double cutoff) {
+  for (int j = std::max(0, i - 1); j <= std::min(ch->n - 2, i + 1); ++j)
+    if (ch->pend[j].on) materialize_pair<T>(ch, j);
+  Pend &p = ch->pend[i];
+  p.on = true;
+  p.t.assign(t, t + 32 * K);
+  p.K = K;
+  p.cutoff = cutoff;
+  ch->bond[i] = 1;
+}
+
+// TNNOptimizer.py:87-108, with pending pairs fused (see file header)
+template <typename T> static void qr_sweep(mpdo_chain_s *ch) {
+  Engine &e = ch->eng->e;
+  const int n = ch->n;
+  DBuf<cx<T>> Rprev;
+  int Rrows = 0, Rcols = 0;
+  auto absorb = [&](int i) -> DBuf<cx<T>> {
+    // returns R_prev . A_i as a new buffer (b x 2 a r)
+    const Site s = ch->s[i];
+    DBuf<cx<T>> X(e, (size_t)Rrows * 2 * s.a * s.r);
+    gemm<T>(e, Rrows, 2 * s.a * s.r, s.l, RM<T>(Rprev.p, Rcols), RM<T>(site_ptr<T>(ch, i), 2 * s.a * s.r), X.p,
+            2 * s.a * s.r);
+    return X;
+  };
+  for (int i = 0; i < n - 1; ++i) {
+    if (ch->pend[i].on) {
+      Pend pd = ch->pend[i];
+      ch->pend[i].on = false;
+      int b = ch->s[i].l;
+      const int a = ch->s[i].a, m = ch->s[i].r;
+      if (Rprev.p) {
+        DBuf<cx<T>> X = absorb(i);
+        set_site<T>(ch, i, X.release(), Rrows, a, m);
+        b = Rrows;
+        Rprev.reset();
+      }
+      // At[(b,a)][(s,m)]
+      DBuf<cx<T>> At(e, (size_t)b * a * 2 * m);
+      {
+        const int64_t d[4] = {b, a, 2, m};
+        const int64_t st[4] = {(int64_t)2 * a * m, m, (int64_t)a * m, 1};
+        copy4d<T>(e.stream, At.p, site_ptr<T>(ch, i), d, st, 0);
+      }
+      const int mr = b * a, nc = 2 * m, kq = std::min(mr, nc);
+      DBuf<cx<T>> Qp(e, (size_t)mr * kq), Rp(e, (size_t)kq * nc);
+      qr<T>(e, mr, nc, RM<T>(At.p, nc), Qp.p, Rp.p);
+      At.reset();
+      DBuf<cx<T>> Si(e, (size_t)b * 2 * a * 2 * kq);
+      blockdiag2<T>(e.stream, Si.p, Qp.p, b, a, kq);
+      set_site<T>(ch, i, Si.release(), b, a, 2 * kq);
+      // W[s][k][t][c][r] = sum_m R'[k][s*m + m'] A_{i+1}[m'][t][c][r]
+      const Site B = ch->s[i + 1];
+      const int c = B.a, r = B.r, K = pd.K;
+      const int ncol = 2 * c * r;
+      DBuf<cx<T>> W(e, (size_t)2 * kq * ncol);
+      gemm<T>(e, kq, ncol, m, View<T>{Rp.p, (int64_t)m, 1, nc, 0, 1, 0}, RM<T>(site_ptr<T>(ch, i + 1), ncol), W.p,
+              ncol, 2, (int64_t)kq * ncol);
+      DBuf<cx<T>> Z(e, (size_t)2 * kq * 2 * c * K * r);
+      mix2q<T>(e.stream, W.p, Z.p, kq, c, r, pd.t.data(), K);
+      set_site<T>(ch, i + 1, Z.release(), 2 * kq, c * K, r);
+      continue;
+    }
+    if (Rprev.p) {
+      const Site s = ch->s[i];
+      DBuf<cx<T>> X = absorb(i);
+      set_site<T>(ch, i, X.release(), Rrows, s.a, s.r);
+      Rprev.reset();
+    }
+    const Site s = ch->s[i];
+    const int mr = s.l * 2 * s.a, nc = s.r, kq = std::min(mr, nc);
+    DBuf<cx<T>> Q(e, (size_t)mr * kq), R(e, (size_t)kq * nc);
+    qr<T>(e, mr, nc, RM<T>(site_ptr<T>(ch, i), nc), Q.p, R.p);
+    set_site<T>(ch, i, Q.release(), s.l, s.a, kq);
+    Rprev = std::move(R);
+    Rrows = kq; Rcols = nc;
+  }
+  if (Rprev.p) {
+    const Site s = ch->s[n - 1];
+    DBuf<cx<T>> X = absorb(n - 1);
+    set_site<T>(ch, n - 1, X.release(), Rrows, s.a, s.r);
+  }
+}
+
+// TNNOptimizer.py:111-134
+template <typename T> static void svd_sweep(mpdo_chain_s *ch, int chi, double max_err, double *wdev) {
+  Engine &e = ch->eng->e;
+  for (int idx = ch->n - 1; idx >= 1; --idx) {
+    const Site P = ch->s[idx - 1], S = ch->s[idx];
+    const int b = S.l, Nc = 2 * S.a * S.r;
+    const int rows_prev = P.l * 2 * P.a;
+    auto keep_fn = [&](const T *s_dev, int) -> int {
+      const int nsv = std::min(rows_prev, Nc);
+      const int cap = chi > 0 ? std::min(chi, nsv) : nsv;
+      if (max_err < 0) return cap;
+      std::vector<T> s(std::min(b, Nc));
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(s.data(), s_dev, s.size() * sizeof(T), cudaMemcpyDeviceToHost, e.stream));
+      MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+      return error_rule_keep<T>(s, nsv, cap, max_err, true);
+    };
+    DBuf<cx<T>> Lf, Rf;
+    int keep = 0;
+    svd_split<T>(e, site_ptr<T>(ch, idx), b, Nc, keep_fn, Lf, Rf, keep, wdev ? wdev + 2 * (idx - 1) : nullptr);
+    DBuf<cx<T>> NP(e, (size_t)rows_prev * keep);
+    gemm<T>(e, rows_prev, keep, b, RM<T>(site_ptr<T>(ch, idx - 1), b), RM<T>(Lf.p, keep), NP.p, keep);
+    set_site<T>(ch, idx - 1, NP.release(), P.l, P.a, keep);
+    set_site<T>(ch, idx, Rf.release(), keep, S.a, S.r);
+  }
+}
+
+// TNNOptimizer.py:164-197: per site, SVD of (l,s,r) x a keeping kappa; the
+// site becomes U S = A V[:, :keep].  V comes from QR of A and one-sided
+// Jacobi on R.
+template <typename T> static void kappa_pass(mpdo_chain_s *ch, int kappa, double max_err) {
+  Engine &e = ch->eng->e;
+  if (kappa <= 0 && max_err < 0) return;
+  for (int i = 0; i < ch->n; ++i) {
+    const Site s = ch->s[i];
+    if (s.a == 1 || (kappa > 0 && s.a <= kappa)) continue;
+    const int rows = s.l * 2 * s.r, a = s.a;
+    DBuf<cx<T>> Am(e, (size_t)rows * a);
+    {
+      const int64_t d[4] = {s.l, 2, s.r, a};
+      const int64_t st[4] = {(int64_t)2 * a * s.r, (int64_t)a * s.r, 1, s.r};
+      copy4d<T>(e.stream, Am.p, site_ptr<T>(ch, i), d, st, 0);
+    }
+    DBuf<cx<T>> V;
+    DBuf<T> sg;
+    right_svd<T>(e, rows, a, RM<T>(Am.p, a), V, sg);
+    const int nsv = std::min(rows, a);
+    int keep = kappa > 0 ? std::min(kappa, nsv) : nsv;
+    if (max_err >= 0) {
+      std::vector<T> sv(nsv);
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(sv.data(), sg.p, nsv * sizeof(T), cudaMemcpyDeviceToHost, e.stream));
+      MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+      keep = error_rule_keep<T>(sv, nsv, keep, max_err, true);
+    }
+    DBuf<cx<T>> NM(e, (size_t)rows * keep);
+    gemm<T>(e, rows, keep, a, RM<T>(Am.p, a), CM<T>(V.p, a), NM.p, keep);
+    DBuf<cx<T>> NS(e, (size_t)rows * keep);
+    {
+      const int64_t d[4] = {s.l, 2, keep, s.r};
+      const int64_t st[4] = {(int64_t)2 * s.r * keep, (int64_t)s.r * keep, 1, keep};
+      copy4d<T>(e.stream, NS.p, NM.p, d, st, 0);
+    }
+    set_site<T>(ch, i, NS.release(), s.l, keep, s.r);
+  }
+}
+
+static bool connected(mpdo_chain_s *ch) {
+  for (int i = 0; i + 1 < ch->n; ++i)
+    if (!ch->bond[i]) return false;
+  return true;
+}
+
+template <typename T>
+static void truncate_layer(mpdo_chain_s *ch, int chi, int kappa, double max_err, int noisy, double *disc_out) {
+  Engine &e = ch->eng->e;
+  if (!connected(ch)) return;  // Circuit.py:477 checkConnectivity
+  DBuf<double> w;
+  if (chi > 0 || max_err >= 0) {
+    if (disc_out && ch->n > 1) w = DBuf<double>(e, (size_t)2 * (ch->n - 1));
+    if (!e.fuse_2q) materialize_all<T>(ch);
+    qr_sweep<T>(ch);
+    svd_sweep<T>(ch, chi, max_err, w.p);
+  }
+  if (noisy) {
+    materialize_all<T>(ch);
+    kappa_pass<T>(ch, kappa, max_err);
+  }
+  if (disc_out && ch->n > 1) {
+    if (w.p) {
+      std::vector<double> h(2 * (ch->n - 1));
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), w.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
+      MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+      for (int i = 0; i < ch->n - 1; ++i) disc_out[i] = h[2 * i + 1] > 0 ? (h[2 * i + 1] - h[2 * i]) / h[2 * i + 1] : 0.0;
+    } else {
+      for (int i = 0; i < ch->n - 1; ++i) disc_out[i] = 0.0;
+    }
+  }
+}
+
+// ------------------------------------------------------------ readout ---
+// Environment E[P][r][r'] sweeping left to right.  P enumerates, per kept
+// site, the (ket x, bra y) pair (interleaved) -- or just x for diagonal
+// readouts.
+template <typename T> struct Env {
+  DBuf<cx<T>> E;
+  int64_t P = 1;
+  int r = 1;
+};
+
+// one site of an environment sweep.  mode 0: trace (optionally with op on the
+// ket side), 1: open (x, y), 2: open diagonal (x = y).
+template <typename T>
+static void env_step(Engine &e, Env<T> &env, const cx<T> *A, const Site &s, int mode, const double *op) {
+  const int l = s.l, a = s.a, R = s.r;
+  if (l != env.r) fail(MPDO_ERR_BAD_SHAPE, "bond mismatch in readout");
+  const int64_t P = env.P;
+  const cx<T> *Aket = A;
+  DBuf<cx<T>> Aop;
+  if (op) {
+    Aop = DBuf<cx<T>>(e, s.elems());
+    apply_op_site<T>(e.stream, A, Aop.p, l, a, R, op);
+    Aket = Aop.p;
+  }
+  // F[P][x][l'][a][r] = sum_l E[P][l][l'] Aket[l][x][a][r]
+  DBuf<cx<T>> F(e, (size_t)P * 2 * l * a * R);
+  const int64_t aR = (int64_t)a * R;
+  for (int x = 0; x < 2; ++x)
+    gemm<T>(e, l, (int)aR, l, CM<T>(env.E.p, l, 0, (int64_t)l * l), RM<T>(Aket + x * aR, 2 * aR), F.p + x * l * aR,
+            aR, (int)P, (int64_t)2 * l * aR);
+  // Ap[y][l'][a][r'] (bra side, conjugated in the product)
+  DBuf<cx<T>> Ap(e, s.elems());
+  {
+    const int64_t d[4] = {2, l, a, R};
+    const int64_t st[4] = {aR, 2 * aR, R, 1};
+    copy4d<T>(e.stream, Ap.p, A, d, st, 0);
+  }
+  const int64_t kdim = (int64_t)l * a;
+  if (mode == 0) {
+    DBuf<cx<T>> En(e, (size_t)P * R * R);
+    // E'[P][r][r'] = sum_{(x,l',a)} F[P][(x,l',a)][r] conj(Ap[(x,l',a)][r'])
+    gemm<T>(e, R, R, (int)(2 * kdim), CM<T>(F.p, R, 0, (int64_t)2 * l * aR), RM<T>(Ap.p, R, 1), En.p, R, (int)P,
+            (int64_t)R * R);
+    env.E = std::move(En);
+  } else if (mode == 1) {
+    DBuf<cx<T>> En(e, (size_t)P * 4 * R * R);
+    for (int x = 0; x < 2; ++x)
+      for (int y = 0; y < 2; ++y)
+        gemm<T>(e, R, R, (int)kdim, CM<T>(F.p + x * l * aR, R, 0, (int64_t)2 * l * aR),
+                RM<T>(Ap.p + y * l * aR, R, 1), En.p + (x * 2 + y) * (int64_t)R * R, R, (int)P, (int64_t)4 * R * R);
+    env.E = std::move(En);
+    env.P = P * 4;
+  } else {
+    DBuf<cx<T>> En(e, (size_t)P * 2 * R * R);
+    for (int x = 0; x < 2; ++x)
+      gemm<T>(e, R, R, (int)kdim, CM<T>(F.p + x * l * aR, R, 0, (int64_t)2 * l * aR),
+              RM<T>(Ap.p + x * l * aR, R, 1), En.p + x * (int64_t)R * R, R, (int)P, (int64_t)2 * R * R);
+    env.E = std::move(En);
+    env.P = P * 2;
+  }
+  env.r = R;
+}
+
+template <typename T> static Env<T> env_start(Engine &e) {
+  Env<T> env;
+  env.E = DBuf<cx<T>>(e, 1);
+  std::vector<cx<T>> one(1, cmk<T>(T(1), T(0)));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(env.E.p, one.data(), sizeof(cx<T>), cudaMemcpyHostToDevice, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  return env;
+}
+
+template <typename T> static std::vector<cx<T>> env_fetch(Engine &e, Env<T> &env) {
+  std::vector<cx<T>> h((size_t)env.P * env.r * env.r);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), env.E.p, h.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  return h;
+}
+
+static void check_keep(mpdo_chain_s *ch, const int *keep, int m, int maxm) {
+  if (m < 0 || m > maxm) fail(MPDO_ERR_INVALID, "too many kept qubits for a dense readout");
+  for (int j = 0; j < m; ++j) {
+    if (keep[j] < 0 || keep[j] >= ch->n) fail(MPDO_ERR_INVALID, "qubit index out of range");
+    if (j && keep[j] <= keep[j - 1]) fail(MPDO_ERR_INVALID, "kept qubits must be strictly ascending");
+  }
+}
+
+template <typename T> static void reduced_dm(mpdo_chain_s *ch, const int *keep, int m, double *out) {
+  Engine &e = ch->eng->e;
+  check_keep(ch, keep, m, 14);
+  materialize_all<T>(ch);
+  Env<T> env = env_start<T>(e);
+  int j = 0;
+  for (int k = 0; k < ch->n; ++k) {
+    const bool open = (j < m && keep[j] == k);
+    if (open) ++j;
+    env_step<T>(e, env, site_ptr<T>(ch, k), ch->s[k], open ? 1 : 0, nullptr);
+  }
+  std::vector<cx<T>> h = env_fetch<T>(e, env);
+  const int64_t D = (int64_t)1 << m;
+  // P index = interleaved (x0, y0, x1, y1, ...) with x0 most significant
+  for (int64_t p = 0; p < D * D; ++p) {
+    int64_t row = 0, col = 0;
+    for (int q = 0; q < m; ++q) {
+      const int64_t bits = (p >> (2 * (m - 1 - q))) & 3;
+      row = (row << 1) | (bits >> 1);
+      col = (col << 1) | (bits & 1);
+    }
+    out[2 * (row * D + col)] = (double)h[p].x;
+    out[2 * (row * D + col) + 1] = (double)h[p].y;
+  }
+}
+
+template <typename T> static void probs(mpdo_chain_s *ch, const int *keep, int m, double *out) {
+  Engine &e = ch->eng->e;
+  check_keep(ch, keep, m, 24);
+  materialize_all<T>(ch);
+  Env<T> env = env_start<T>(e);
+  int j = 0;
+  for (int k = 0; k < ch->n; ++k) {
+    const bool open = (j < m && keep[j] == k);
+    if (open) ++j;
+    env_step<T>(e, env, site_ptr<T>(ch, k), ch->s[k], open ? 2 : 0, nullptr);
+  }
+  std::vector<cx<T>> h = env_fetch<T>(e, env);
+  for (int64_t p = 0; p < ((int64_t)1 << m); ++p) out[p] = (double)h[p].x;
+}
+
+template <typename T> static double expect_ops(mpdo_chain_s *ch, const int *sites, const double *ops, int m) {
+  Engine &e = ch->eng->e;
+  materialize_all<T>(ch);
+  std::vector<const double *> opat(ch->n, nullptr);
+  for (int j = 0; j < m; ++j) {
+    if (sites[j] < 0 || sites[j] >= ch->n) fail(MPDO_ERR_INVALID, "qubit index out of range");
+    if (opat[sites[j]]) fail(MPDO_ERR_INVALID, "operator sites must be distinct");
+    opat[sites[j]] = ops + 8 * j;
+  }
+  Env<T> env = env_start<T>(e);
+  for (int k = 0; k < ch->n; ++k) env_step<T>(e, env, site_ptr<T>(ch, k), ch->s[k], 0, opat[k]);
+  std::vector<cx<T>> h = env_fetch<T>(e, env);
+  return (double)h[0].x;
+}
+
+// ------------------------------------------------------------ status ----
+static int *status_slot(Engine &e, int count) {
+  if (e.status_used + count > e.status_cap) check_status(e);
+  int *p = e.d_status + e.status_used;
+  e.status_used += count;
+  return p;
+}
+static void check_status(Engine &e) {
+  if (e.status_used == 0) return;
+  std::vector<int> h(e.status_used);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), e.d_status, h.size() * sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  for (int v : h)
+    if (v != 0 && e.first_status == 0) e.first_status = v;
+  MPDO_CUDA_CHECK(cudaMemsetAsync(e.d_status, 0, e.status_cap * sizeof(int), e.stream));
+  e.status_used = 0;
+}
+
+}  // namespace mpdo
+
+// ================================================================ C ABI ====
+using namespace mpdo;
+
+template <typename F> static mpdo_status guard(F &&f) {
+  try {
+    f();
+    return MPDO_OK;
+  } catch (const Error &err) {
+    g_last_error = err.msg;
+    return err.st;
+  } catch (const CudaError &ce) {
+    g_last_error = std::string(ce.expr) + ": " + cudaGetErrorString(ce.err) + " (" + ce.file + ":" +
+                   std::to_string(ce.line) + ")";
+    return MPDO_ERR_CUDA;
+  } catch (const std::exception &ex) {
+    g_last_error = ex.what();
+    return MPDO_ERR_INVALID;
+  }
+}
+
+#define DISPATCH(ch, FN, ...)                        \
+  do {                                               \
+    if ((ch)->dtype == MPDO_C64) FN<float>(__VA_ARGS__); \
+    else FN<double>(__VA_ARGS__);                    \
+  } while (0)
+
+static void need(bool c, const char *msg) {
+  if (!c) fail(MPDO_ERR_INVALID, msg);
+}
+static void set_device(mpdo_engine_s *eng) { MPDO_CUDA_CHECK(cudaSetDevice(eng->e.device)); }
+
+template <typename T>
+static void chain_init(mpdo_chain_s *ch, const double *vec) {
+  Engine &e = ch->eng->e;
+  for (int i = 0; i < ch->n; ++i) {
+    cx<T> h[2] = {cmk<T>((T)vec[4 * i], (T)vec[4 * i + 1]), cmk<T>((T)vec[4 * i + 2], (T)vec[4 * i + 3])};
+    cx<T> *p = static_cast<cx<T> *>(dalloc(e, 2 * sizeof(cx<T>)));
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(p, h, sizeof(h), cudaMemcpyHostToDevice, e.stream));
+    ch->s[i] = Site{p, 1, 1, 1};
+  }
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+}
+
+template <typename T> static void read_site(mpdo_chain_s *ch, int site, double *out) {
+  Engine &e = ch->eng->e;
+  materialize_touching<T>(ch, site);
+  const size_t n = ch->s[site].elems();
+  std::vector<cx<T>> h(n);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), ch->s[site].p, n * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  for (size_t i = 0; i < n; ++i) { out[2 * i] = h[i].x; out[2 * i + 1] = h[i].y; }
+}
+
+template <typename T> static void write_site(mpdo_chain_s *ch, int site, const int dims[4], const double *in) {
+  Engine &e = ch->eng->e;
+  materialize_touching<T>(ch, site);
+  const size_t n = (size_t)dims[0] * 2 * dims[2] * dims[3];
+  std::vector<cx<T>> h(n);
+  for (size_t i = 0; i < n; ++i) h[i] = cmk<T>((T)in[2 * i], (T)in[2 * i + 1]);
+  cx<T> *p = static_cast<cx<T> *>(dalloc(e, n * sizeof(cx<T>)));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(p, h.data(), n * sizeof(cx<T>), cudaMemcpyHostToDevice, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  set_site<T>(ch, site, p, dims[0], dims[2], dims[3]);
+}
+
+
+// ------------------------------------------------------- test hooks -----
+template <typename T> static std::vector<cx<T>> to_cx(const double *h, size_t n) {
+  std::vector<cx<T>> v(n);
+  for (size_t i = 0; i < n; ++i) v[i] = cmk<T>((T)h[2 * i], (T)h[2 * i + 1]);
+  return v;
+}
+template <typename T> static void from_cx(const std::vector<cx<T>> &v, double *h) {
+  for (size_t i = 0; i < v.size(); ++i) { h[2 * i] = v[i].x; h[2 * i + 1] = v[i].y; }
+}
+template <typename T>
+static void debug_qr(Engine &e, int m, int n, const double *a, double *q, double *r) {
+  const int k = std::min(m, n);
+  std::vector<cx<T>> ha = to_cx<T>(a, (size_t)m * n);
+  DBuf<cx<T>> A(e, ha.size()), Q(e, (size_t)m * k), R(e, (size_t)k * n);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(A.p, ha.data(), ha.size() * sizeof(cx<T>), cudaMemcpyHostToDevice, e.stream));
+  qr<T>(e, m, n, RM<T>(A.p, n), Q.p, R.p);
+  std::vector<cx<T>> hq((size_t)m * k), hr((size_t)k * n);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(hq.data(), Q.p, hq.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(hr.data(), R.p, hr.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  from_cx<T>(hq, q);
+  from_cx<T>(hr, r);
+}
+template <typename T>
+static void debug_split(Engine &e, int Mr, int Nc, int keep, const double *y, double *l, double *r) {
+  std::vector<cx<T>> hy = to_cx<T>(y, (size_t)Mr * Nc);
+  DBuf<cx<T>> Y(e, hy.size()), Lf, Rf;
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(Y.p, hy.data(), hy.size() * sizeof(cx<T>), cudaMemcpyHostToDevice, e.stream));
+  int kept = 0;
+  svd_split<T>(e, Y.p, Mr, Nc, [&](const T *, int) { return keep; }, Lf, Rf, kept, nullptr);
+  std::vector<cx<T>> hl((size_t)Mr * keep), hr((size_t)keep * Nc);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(hl.data(), Lf.p, hl.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(hr.data(), Rf.p, hr.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  from_cx<T>(hl, l);
+  from_cx<T>(hr, r);
+}
+template <typename T>
+static void debug_svd(Engine &e, int m, int n, const double *a, double *w, double *sv) {
+  std::vector<cx<T>> ha = to_cx<T>(a, (size_t)m * n);
+  DBuf<cx<T>> A(e, ha.size()), W;
+  DBuf<T> S;
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(A.p, ha.data(), ha.size() * sizeof(cx<T>), cudaMemcpyHostToDevice, e.stream));
+  right_svd<T>(e, m, n, RM<T>(A.p, n), W, S);
+  std::vector<cx<T>> hw((size_t)n * n);
+  std::vector<T> hs(n);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(hw.data(), W.p, hw.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(hs.data(), S.p, n * sizeof(T), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  from_cx<T>(hw, w);
+  for (int i = 0; i < n; ++i) sv[i] = hs[i];
+}
+
+extern "C" {
+
+int mpdo_abi_version(void) { return MPDO_ABI_VERSION; }
+
+const char *mpdo_status_string(mpdo_status s) {
+  switch (s) {
+    case MPDO_OK: return "ok";
+    case MPDO_ERR_INVALID: return "invalid argument";
+    case MPDO_ERR_BAD_SHAPE: return "bad shape";
+    case MPDO_ERR_OOM: return "out of device memory";
+    case MPDO_ERR_CUDA: return "CUDA error";
+    case MPDO_ERR_NOT_CONVERGED: return "Jacobi iteration did not converge";
+    case MPDO_ERR_NONFINITE: return "non-finite value in a factorisation";
+    case MPDO_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+const char *mpdo_last_error(void) { return g_last_error.c_str(); }
+
+mpdo_status mpdo_engine_create(int device, mpdo_engine_t *out) {
+  return guard([&] {
+    need(out != nullptr, "out is NULL");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      fail(MPDO_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    need(device >= 0 && device < ndev, "device index out of range");
+    auto eng = std::make_unique<mpdo_engine_s>();
+    Engine &e = eng->e;
+    e.device = device;
+    MPDO_CUDA_CHECK(cudaSetDevice(device));
+    MPDO_CUDA_CHECK(cudaStreamCreateWithFlags(&e.own_stream, cudaStreamNonBlocking));
+    e.stream = e.own_stream;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    MPDO_CUDA_CHECK(cudaMemPoolCreate(&e.pool, &props));
+    uint64_t thr = UINT64_MAX;
+    MPDO_CUDA_CHECK(cudaMemPoolSetAttribute(e.pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    MPDO_CUDA_CHECK(cudaMalloc(&e.d_status, e.status_cap * sizeof(int)));
+    MPDO_CUDA_CHECK(cudaMemsetAsync(e.d_status, 0, e.status_cap * sizeof(int), e.stream));
+    *out = eng.release();
+  });
+}
+
+mpdo_status mpdo_engine_destroy(mpdo_engine_t eng) {
+  return guard([&] {
+    if (!eng) return;
+    Engine &e = eng->e;
+    cudaSetDevice(e.device);
+    cudaStreamSynchronize(e.stream);
+    if (e.d_status) cudaFree(e.d_status);
+    if (e.pool) cudaMemPoolDestroy(e.pool);
+    if (e.own_stream) cudaStreamDestroy(e.own_stream);
+    delete eng;
+  });
+}
+
+mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream) {
+  return guard([&] {
+    need(eng != nullptr, "engine is NULL");
+    Engine &e = eng->e;
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+    e.stream = stream ? static_cast<cudaStream_t>(stream) : e.own_stream;
+  });
+}
+
+mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double value) {
+  return guard([&] {
+    need(eng && name, "NULL argument");
+    const std::string k(name);
+    Engine &e = eng->e;
+    if (k == "fuse_2q") e.fuse_2q = value != 0;
+    else if (k == "max_sweeps") { need(value >= 1 && value <= 1000, "max_sweeps out of range"); e.max_sweeps = (int)value; }
+    else fail(MPDO_ERR_INVALID, "unknown option: " + k);
+  });
+}
+
+mpdo_status mpdo_engine_sync(mpdo_engine_t eng) {
+  mpdo_status st = guard([&] {
+    need(eng != nullptr, "engine is NULL");
+    set_device(eng);
+    check_status(eng->e);
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(eng->e.stream));
+    MPDO_CUDA_CHECK(cudaGetLastError());
+  });
+  if (st != MPDO_OK) return st;
+  const int fs = eng->e.first_status;
+  eng->e.first_status = 0;
+  if (fs == DEV_NOT_CONVERGED) { g_last_error = "Jacobi sweep limit reached"; return MPDO_ERR_NOT_CONVERGED; }
+  if (fs == DEV_NONFINITE) { g_last_error = "non-finite value met in a factorisation"; return MPDO_ERR_NONFINITE; }
+  return MPDO_OK;
+}
+
+mpdo_status mpdo_engine_launch_count(mpdo_engine_t eng, uint64_t *count) {
+  return guard([&] {
+    need(eng != nullptr && count != nullptr, "NULL argument");
+    *count = launch_count();
+  });
+}
+
+
+mpdo_status mpdo_chain_create(mpdo_engine_t eng, int n, int dtype, const double *vectors, int connected_,
+                              mpdo_chain_t *out) {
+  return guard([&] {
+    need(eng && vectors && out, "NULL argument");
+    need(n >= 1, "n must be >= 1");
+    need(dtype == MPDO_C64 || dtype == MPDO_C128, "dtype must be MPDO_C64 or MPDO_C128");
+    set_device(eng);
+    auto ch = std::make_unique<mpdo_chain_s>();
+    ch->eng = eng;
+    ch->n = n;
+    ch->dtype = dtype;
+    ch->s.assign(n, Site{});
+    ch->bond.assign(std::max(0, n - 1), connected_ ? 1 : 0);
+    ch->pend.assign(std::max(0, n - 1), Pend{});
+    if (dtype == MPDO_C64) chain_init<float>(ch.get(), vectors);
+    else chain_init<double>(ch.get(), vectors);
+    *out = ch.release();
+  });
+}
+
+mpdo_status mpdo_chain_destroy(mpdo_chain_t ch) {
+  return guard([&] {
+    if (!ch) return;
+    set_device(ch->eng);
+    for (auto &s : ch->s)
+      if (s.p) cudaFreeAsync(s.p, ch->eng->e.stream);
+    delete ch;
+  });
+}
+
+mpdo_status mpdo_chain_clone(mpdo_chain_t src, mpdo_chain_t *out) {
+  return guard([&] {
+    need(src && out, "NULL argument");
+    set_device(src->eng);
+    Engine &e = src->eng->e;
+    auto ch = std::make_unique<mpdo_chain_s>(*src);
+    const size_t esz = src->dtype == MPDO_C64 ? 8 : 16;
+    for (int i = 0; i < ch->n; ++i) {
+      void *p = dalloc(e, src->s[i].elems() * esz);
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(p, src->s[i].p, src->s[i].elems() * esz, cudaMemcpyDeviceToDevice, e.stream));
+      ch->s[i].p = p;
+    }
+    *out = ch.release();
+  });
+}
+
+mpdo_status mpdo_chain_num_sites(mpdo_chain_t ch, int *n) {
+  return guard([&] {
+    need(ch && n, "NULL argument");
+    *n = ch->n;
+  });
+}
+
+mpdo_status mpdo_chain_site_dims(mpdo_chain_t ch, int site, int dims[4]) {
+  return guard([&] {
+    need(ch && dims, "NULL argument");
+    need(site >= 0 && site < ch->n, "site out of range");
+    set_device(ch->eng);
+    DISPATCH(ch, materialize_touching, ch, site);
+    dims[0] = ch->s[site].l; dims[1] = 2; dims[2] = ch->s[site].a; dims[3] = ch->s[site].r;
+  });
+}
+
+mpdo_status mpdo_chain_bond_present(mpdo_chain_t ch, int bond, int *present) {
+  return guard([&] {
+    need(ch && present, "NULL argument");
+    need(bond >= 0 && bond < ch->n - 1, "bond out of range");
+    *present = ch->bond[bond] ? 1 : 0;
+  });
+}
+
+
+mpdo_status mpdo_chain_read_site(mpdo_chain_t ch, int site, double *host_out) {
+  return guard([&] {
+    need(ch && host_out, "NULL argument");
+    need(site >= 0 && site < ch->n, "site out of range");
+    set_device(ch->eng);
+    DISPATCH(ch, read_site, ch, site, host_out);
+  });
+}
+
+
+mpdo_status mpdo_chain_write_site(mpdo_chain_t ch, int site, const int dims[4], const double *host_in) {
+  return guard([&] {
+    need(ch && dims && host_in, "NULL argument");
+    need(site >= 0 && site < ch->n, "site out of range");
+    need(dims[0] >= 1 && dims[1] == 2 && dims[2] >= 1 && dims[3] >= 1, "bad site dims");
+    set_device(ch->eng);
+    DISPATCH(ch, write_site, ch, site, dims, host_in);
+  });
+}
+
+mpdo_status mpdo_apply_1q(mpdo_chain_t ch, int site, const double *kraus, int K) {
+  return guard([&] {
+    need(ch && kraus, "NULL argument");
+    need(site >= 0 && site < ch->n, "Qubit index out of range");
+    need(K >= 1 && K <= 16, "K must be in [1, 16]");
+    set_device(ch->eng);
+    DISPATCH(ch, apply_1q, ch, site, kraus, K);
+  });
+}
+
+mpdo_status mpdo_apply_2q(mpdo_chain_t ch, int site_min, const double *kraus, int K, double abs_cutoff) {
+  return guard([&] {
+    need(ch && kraus, "NULL argument");
+    need(ch->n >= 2 && site_min >= 0 && site_min < ch->n - 1, "Qubit index out of range");
+    need(K >= 1 && K <= 16, "K must be in [1, 16]");
+    set_device(ch->eng);
+    DISPATCH(ch, apply_2q, ch, site_min, kraus, K, abs_cutoff);
+  });
+}
+
+mpdo_status mpdo_truncate(mpdo_chain_t ch, int chi, int kappa, double max_err, int noisy, double *discarded_out) {
+  return guard([&] {
+    need(ch != nullptr, "NULL argument");
+    set_device(ch->eng);
+    DISPATCH(ch, truncate_layer, ch, chi, kappa, max_err, noisy, discarded_out);
+  });
+}
+
+mpdo_status mpdo_kappa_truncate(mpdo_chain_t ch, int kappa, double max_err) {
+  return guard([&] {
+    need(ch != nullptr, "NULL argument");
+    set_device(ch->eng);
+    DISPATCH(ch, materialize_all, ch);
+    DISPATCH(ch, kappa_pass, ch, kappa, max_err);
+  });
+}
+
+mpdo_status mpdo_reduced_dm(mpdo_chain_t ch, const int *keep, int m, double *host_out) {
+  return guard([&] {
+    need(ch && host_out && (keep || m == 0), "NULL argument");
+    set_device(ch->eng);
+    DISPATCH(ch, reduced_dm, ch, keep, m, host_out);
+  });
+}
+
+mpdo_status mpdo_probs(mpdo_chain_t ch, const int *keep, int m, double *host_out) {
+  return guard([&] {
+    need(ch && host_out && (keep || m == 0), "NULL argument");
+    set_device(ch->eng);
+    DISPATCH(ch, probs, ch, keep, m, host_out);
+  });
+}
+
+mpdo_status mpdo_expect_ops(mpdo_chain_t ch, const int *sites, const double *ops, int m, double *out) {
+  return guard([&] {
+    need(ch && out && ((sites && ops) || m == 0), "NULL argument");
+    set_device(ch->eng);
+    if (ch->dtype == MPDO_C64) *out = expect_ops<float>(ch, sites, ops, m);
+    else *out = expect_ops<double>(ch, sites, ops, m);
+  });
+}
+
+mpdo_status mpdo_expect_pauli_batch(mpdo_chain_t ch, const int8_t *paulis, int nterms, double *out) {
+  static const double PM[4][8] = {{1, 0, 0, 0, 0, 0, 1, 0},
+                                  {0, 0, 1, 0, 1, 0, 0, 0},
+                                  {0, 0, 0, -1, 0, 1, 0, 0},
+                                  {1, 0, 0, 0, 0, 0, -1, 0}};
+  return guard([&] {
+    need(ch && out && (paulis || nterms == 0), "NULL argument");
+    set_device(ch->eng);
+    for (int t = 0; t < nterms; ++t) {
+      std::vector<int> sites;
+      std::vector<double> ops;
+      for (int q = 0; q < ch->n; ++q) {
+        const int p = paulis[(size_t)t * ch->n + q];
+        need(p >= 0 && p <= 3, "Pauli code must be 0..3");
+        if (p == 0) continue;
+        sites.push_back(q);
+        ops.insert(ops.end(), PM[p], PM[p] + 8);
+      }
+      if (ch->dtype == MPDO_C64) out[t] = expect_ops<float>(ch, sites.data(), ops.data(), (int)sites.size());
+      else out[t] = expect_ops<double>(ch, sites.data(), ops.data(), (int)sites.size());
+    }
+  });
+}
+
+mpdo_status mpdo_debug_qr(mpdo_engine_t eng, int dtype, int m, int n, const double *a, double *q, double *r) {
+  return guard([&] {
+    need(eng && a && q && r && m > 0 && n > 0, "bad argument");
+    set_device(eng);
+    if (dtype == MPDO_C64) debug_qr<float>(eng->e, m, n, a, q, r);
+    else debug_qr<double>(eng->e, m, n, a, q, r);
+  });
+}
+
+mpdo_status mpdo_debug_split(mpdo_engine_t eng, int dtype, int m, int n, int keep, const double *y, double *l,
+                             double *r) {
+  return guard([&] {
+    need(eng && y && l && r && m > 0 && n > 0 && keep > 0, "bad argument");
+    set_device(eng);
+    if (dtype == MPDO_C64) debug_split<float>(eng->e, m, n, keep, y, l, r);
+    else debug_split<double>(eng->e, m, n, keep, y, l, r);
+  });
+}
+
+mpdo_status mpdo_debug_svd(mpdo_engine_t eng, int dtype, int m, int n, const double *a, double *w,
+                           double *sigma) {
+  return guard([&] {
+    need(eng && a && w && sigma && m > 0 && n > 0 && n <= 1024, "bad argument");
+    set_device(eng);
+    if (dtype == MPDO_C64) debug_svd<float>(eng->e, m, n, a, w, sigma);
+    else debug_svd<double>(eng->e, m, n, a, w, sigma);
+  });
+}
+
+}  // extern "C"

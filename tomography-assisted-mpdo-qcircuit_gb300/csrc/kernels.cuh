@@ -1,0 +1,102 @@
+// Host-side launchers of the engine's CUDA kernels.  All launchers enqueue on
+// the given stream and never synchronise.
+#pragma once
+
+#include "common.cuh"
+
+namespace mpdo {
+
+// ---------------------------------------------------------------- GEMM ----
+// C[b](i,j) = alpha * sum_k A[b](i,k) B[b](k,j) + beta * C[b](i,j)
+// for i < M, j < N, b < batch; A, B are strided (optionally conjugated) views;
+// C is written with strides (c_rs, c_cs, c_bs).  beta == 0 never reads C.
+template <typename T>
+void cgemm(cudaStream_t st, int M, int N, int K, int batch, cx<T> alpha, const View<T> &A,
+           const View<T> &B, cx<T> beta, cx<T> *C, int64_t c_rs, int64_t c_cs, int64_t c_bs,
+           cx<T> *splitk_ws = nullptr, size_t splitk_ws_elems = 0);
+
+// -------------------------------------------------- Householder QR (TSQR) --
+// Factor nchunks independent row blocks of an m x n matrix given by `in`
+// (chunk c holds rows [c*mc, min(m, (c+1)*mc))).  Per chunk: the Householder
+// vectors and tau are kept in `vws` (mc x n column-major per chunk) and `tau`
+// (n per chunk); R_c (kc x n, kc = min(rows_c, n)) is written row-major into
+// `rstack` at row offset c*n (rows kc..n-1 of the slot are zero-filled).
+template <typename T>
+void qr_factor_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const View<T> &in, cx<T> *vws,
+                      cx<T> *tau, cx<T> *rstack);
+
+// Q_c = H_c(0) ... H_c(kc-1) [B_c; 0] for every chunk, where B_c is the
+// kc x nq block of `bin` (row-major, leading dimension ldb) starting at row
+// c*n, or the identity when bin == nullptr.  Q_c is written into `qout`
+// (row-major m x nq, leading dimension ldq) at rows [c*mc, c*mc + rows_c).
+template <typename T>
+void qr_apply_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const cx<T> *vws, const cx<T> *tau,
+                     const cx<T> *bin, int64_t ldb, int nq, cx<T> *qout, int64_t ldq);
+
+// ------------------------------------------------- one-sided Jacobi SVD ---
+// For each of `batch` matrices X_b (m x n, given by `in`), orthogonalise the
+// columns by Hestenes-Jacobi rotations: X W = U diag(sigma).  Outputs, sorted
+// by sigma descending: U (m x n column-major per batch in `uout`, zero columns
+// where sigma == 0), sigma (n per batch) and, when wout != nullptr, W
+// (n x n column-major per batch).  xws: workspace m x n per batch (may be
+// uout).  wws: workspace n x n per batch when W is wanted.  status[b] gets a
+// DevStatus.
+template <typename T>
+void jacobi_svd(cudaStream_t st, int batch, int m, int n, const View<T> &in, cx<T> *uout, T *sigma,
+                cx<T> *wout, cx<T> *xws, cx<T> *wws, int max_sweeps, int *status);
+
+// --------------------------------------------------- site-tensor kernels --
+// out[l][x][a*K+k][r] = sum_s G[x][s][k] A[l][s][a][r]     (K <= 16)
+template <typename T>
+void kraus1q(cudaStream_t st, const cx<T> *A, cx<T> *out, int L, int Aa, int R, const double *g_host, int K);
+
+// Z[(x,k)][y][(c,kk)][r] = sum_{s,t} Tg[x][y][s][t][kk] W[s][k][t][c][r]
+// W: [2][kr][2][C][R]; Z: [2][kr][2][C*K][R].  (K <= 16)
+template <typename T>
+void mix2q(cudaStream_t st, const cx<T> *W, cx<T> *Z, int kr, int Cc, int R, const double *t_host, int K);
+// Same with a leading batch leg: W [nb][2][kr][2][C][R] -> Z [nb][2][kr][2][C*K][R]
+template <typename T>
+void mix2q_batched(cudaStream_t st, const cx<T> *W, cx<T> *Z, int nb, int kr, int Cc, int R, const double *t_host,
+                   int K);
+
+// Generic strided 4-D copy: dst[i0][i1][i2][i3] (contiguous) = conj?(src[...strided...])
+template <typename T>
+void copy4d(cudaStream_t st, cx<T> *dst, const cx<T> *src, const int64_t dims[4], const int64_t sstr[4],
+            int conj);
+
+// X[i][j] *= f(s[j]) (col scaling) or f(s[i]) (row scaling) for a row-major
+// M x N matrix with leading dimension ld.  mode: 0 = s, 1 = sqrt(s),
+// 2 = 1/sqrt(s), 3 = 1/s; modes 2 and 3 give 0 where s <= rel * s[0]
+// (rel = 1e-6 for fp32, 1e-14 for fp64: singular values at rounding level,
+// whose directions are noise, are dropped instead of amplified).
+template <typename T>
+void scale_matrix(cudaStream_t st, cx<T> *X, int M, int N, int64_t ld, const T *s, int by_row, int mode);
+
+// Block-diagonal embedding: dst[b][x][a][x'*kr + k] = (x == x') * Q[(b*A + a)][k]
+// Q row-major ((B*A) x kr).
+template <typename T>
+void blockdiag2(cudaStream_t st, cx<T> *dst, const cx<T> *Q, int B, int Aa, int kr);
+
+template <typename T>
+void fill_zero(cudaStream_t st, cx<T> *p, size_t n);
+
+// Sum of squares of sigma[0..n) in double; out[0] = kept sum, out[1] = total
+// (kept = first `keep` entries).  Used for the discarded-weight report.
+template <typename T>
+void sigma_weights(cudaStream_t st, const T *sigma, int n, int keep, double *out);
+
+// s[i] = sqrt(max(s[i], 0))
+template <typename T>
+void sqrt_inplace(cudaStream_t st, T *s, int n);
+
+// Readout: E'[D][x][D'][y][r][r'] style environment steps are expressed via
+// cgemm; this kernel contracts a single-site operator into a site:
+// out[l][y][a][r] = sum_x O[y][x] A[l][x][a][r]   (O 2x2 host complex)
+template <typename T>
+void apply_op_site(cudaStream_t st, const cx<T> *A, cx<T> *out, int L, int Aa, int R, const double *o_host);
+
+// Trace of a batch of square matrices: out[b] = sum_i M_b[i][i]  (complex, double accum)
+template <typename T>
+void batched_trace(cudaStream_t st, const cx<T> *M, int n, int64_t ld, int64_t bs, int batch, double2 *out);
+
+}  // namespace mpdo

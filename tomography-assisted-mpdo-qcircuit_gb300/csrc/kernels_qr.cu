@@ -1,0 +1,262 @@
+// Householder QR of row blocks ("chunks") -- the building block of a
+// tall-skinny QR (TSQR) -- and the matching explicit-Q construction.
+//
+// One CTA per chunk.  The chunk (rows_c x n, column-major) lives in shared
+// memory when it fits, otherwise in its global workspace slot (L2 resident).
+// Reflectors follow LAPACK's zlarfg convention (real beta, H = I - tau v v^H,
+// v(0) = 1), so R has a real diagonal of sign -sign(Re alpha); the trailing
+// update applies H^H (zgeqr2), Q is accumulated backwards with H (zungqr).
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <cfloat>
+
+namespace mpdo {
+
+namespace {
+constexpr int QR_NT = 512;
+constexpr size_t SMEM_CAP = 200 * 1024;
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ T block_sum(T v, T *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T s = T(0);
+  if (threadIdx.x < 32) {
+    s = (lane < nw) ? red[lane] : T(0);
+    s = warp_sum(s);
+    if (lane == 0) red[32] = s;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+template <typename T> struct NormalMin;
+template <> struct NormalMin<float> { static constexpr float v = FLT_MIN; };
+template <> struct NormalMin<double> { static constexpr double v = DBL_MIN; };
+
+template <typename T>
+__device__ T block_max(T v, T *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    T s = (lane < nw) ? red[lane] : T(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
+    if (lane == 0) red[32] = s;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+template <typename T, bool SMEM>
+__global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<T> in, cx<T> *vws,
+                                                     cx<T> *tau_out, cx<T> *rstack) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T red[33];
+  __shared__ cx<T> hh[2];  // tau, scale
+  const int c = blockIdx.x;
+  const int r0 = c * mc;
+  const int rows = min(mc, m - r0);
+  const int kc = min(rows, n);
+  cx<T> *Wg = vws + (int64_t)c * mc * n;
+  cx<T> *W = SMEM ? reinterpret_cast<cx<T> *>(smem_raw) : Wg;
+  const int64_t ld = mc;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+
+  for (int64_t idx = tid; idx < (int64_t)rows * n; idx += blockDim.x) {
+    const int i = (int)(idx % rows), j = (int)(idx / rows);
+    W[j * ld + i] = view_ld(in, 0, r0 + i, j);
+  }
+  __syncthreads();
+
+  for (int j = 0; j < kc; ++j) {
+    // scaled 2-norm of the column below the diagonal (as LAPACK's nrm2):
+    // max |x_i| first, then sum (|x_i| / max)^2, so that columns near the
+    // underflow threshold keep an exact norm and the reflector stays unitary
+    T pmax = T(0);
+    for (int i = j + 1 + tid; i < rows; i += blockDim.x) {
+      const cx<T> v = W[j * ld + i];
+      pmax = fmax(pmax, fmax(fabs(v.x), fabs(v.y)));
+    }
+    T amax = block_max(pmax, red);
+    // entries below the smallest normal number are underflow debris: the
+    // column is treated as exactly zero (1/amax would overflow)
+    if (amax < NormalMin<T>::v) {
+      if (amax > T(0))
+        for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = czero<T>();
+      amax = T(0);
+    }
+    T part = T(0);
+    if (amax > T(0)) {
+      const T inv = T(1) / amax;
+      for (int i = j + 1 + tid; i < rows; i += blockDim.x) part += cabs2<T>(cscale<T>(W[j * ld + i], inv));
+    }
+    const T xs = block_sum(part, red);
+    if (tid == 0) {
+      const cx<T> al = W[j * ld + j];
+      cx<T> tau = czero<T>(), scl = czero<T>();
+      const T xnorm = amax * sqrt(xs);
+      const T nrm = hypot(hypot(al.x, al.y), xnorm);
+      if (!(xnorm == T(0) && al.y == T(0)) && nrm >= NormalMin<T>::v) {
+        const T beta = (al.x >= T(0)) ? -nrm : nrm;
+        tau = cmk<T>((beta - al.x) / beta, -al.y / beta);
+        // scl = 1 / (alpha - beta), scaled complex reciprocal
+        const cx<T> d = cmk<T>(al.x - beta, al.y);
+        const T sc = fmax(fabs(d.x), fabs(d.y));
+        const cx<T> ds = cmk<T>(d.x / sc, d.y / sc);
+        const T dd = cabs2<T>(ds);
+        scl = cmk<T>(ds.x / (dd * sc), -ds.y / (dd * sc));
+        W[j * ld + j] = cmk<T>(beta, T(0));
+      }
+      hh[0] = tau; hh[1] = scl;
+      tau_out[(int64_t)c * n + j] = tau;
+    }
+    __syncthreads();
+    const cx<T> tau = hh[0], scl = hh[1];
+    if (tau.x == T(0) && tau.y == T(0)) {
+      // H = I: v below the diagonal must read as zero
+      for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = czero<T>();
+      __syncthreads();
+      continue;
+    }
+    for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = cmul<T>(W[j * ld + i], scl);
+    __syncthreads();
+    const cx<T> ctau = cconj<T>(tau);
+    for (int k = j + 1 + warp; k < n; k += nw) {
+      cx<T> w = (lane == 0) ? W[k * ld + j] : czero<T>();
+      for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(w, W[j * ld + i], W[k * ld + i]);
+      w.x = warp_sum(w.x); w.y = warp_sum(w.y);
+      w = cmul<T>(ctau, w);
+      if (lane == 0) W[k * ld + j] = csub<T>(W[k * ld + j], w);
+      for (int i = j + 1 + lane; i < rows; i += 32) {
+        W[k * ld + i] = csub<T>(W[k * ld + i], cmul<T>(W[j * ld + i], w));
+      }
+    }
+    __syncthreads();
+  }
+  for (int j = kc; j < n; ++j) {
+    if (tid == 0) tau_out[(int64_t)c * n + j] = czero<T>();
+  }
+
+  // R_c into its n-row slot of the stack
+  cx<T> *Rs = rstack + (int64_t)c * n * n;
+  for (int64_t idx = tid; idx < (int64_t)n * n; idx += blockDim.x) {
+    const int i = (int)(idx / n), j = (int)(idx % n);
+    Rs[idx] = (i < kc && j >= i) ? W[j * ld + i] : czero<T>();
+  }
+  if (SMEM) {
+    for (int64_t idx = tid; idx < (int64_t)rows * n; idx += blockDim.x) {
+      const int i = (int)(idx % rows), j = (int)(idx / rows);
+      Wg[j * ld + i] = W[j * ld + i];
+    }
+  }
+}
+
+template <typename T, bool SMEM>
+__global__ void __launch_bounds__(QR_NT) k_qr_apply(int m, int n, int mc, const cx<T> *vws, const cx<T> *tau,
+                                                    const cx<T> *bin, int64_t ldb, int nq, cx<T> *qout,
+                                                    int64_t ldq) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int c = blockIdx.x;
+  const int r0 = c * mc;
+  const int rows = min(mc, m - r0);
+  const int kc = min(rows, n);
+  const cx<T> *V = vws + (int64_t)c * mc * n;
+  const cx<T> *tc = tau + (int64_t)c * n;
+  cx<T> *vcol = reinterpret_cast<cx<T> *>(smem_raw);
+  // B: rows x nq; in shared memory column-major (ld = rows), else in place in
+  // qout (row-major, leading dimension ldq)
+  cx<T> *Bs = vcol + mc;
+  cx<T> *Bg = qout + (int64_t)r0 * ldq;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  auto B = [&](int i, int q) -> cx<T> & { return SMEM ? Bs[(int64_t)q * rows + i] : Bg[(int64_t)i * ldq + q]; };
+
+  for (int64_t idx = tid; idx < (int64_t)rows * nq; idx += blockDim.x) {
+    int i, q;
+    if (SMEM) { i = (int)(idx % rows); q = (int)(idx / rows); } else { i = (int)(idx / nq); q = (int)(idx % nq); }
+    cx<T> v = czero<T>();
+    if (i < kc) {
+      if (bin) v = bin[(int64_t)(c * n + i) * ldb + q];
+      else v = (i == q) ? cmk<T>(T(1), T(0)) : czero<T>();
+    }
+    B(i, q) = v;
+  }
+  __syncthreads();
+  for (int j = kc - 1; j >= 0; --j) {
+    const cx<T> tj = tc[j];
+    if (tj.x == T(0) && tj.y == T(0)) continue;
+    for (int i = j + 1 + tid; i < rows; i += blockDim.x) vcol[i] = V[(int64_t)j * mc + i];
+    __syncthreads();
+    for (int q = warp; q < nq; q += nw) {
+      cx<T> w = (lane == 0) ? B(j, q) : czero<T>();
+      for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(w, vcol[i], B(i, q));
+      w.x = warp_sum(w.x); w.y = warp_sum(w.y);
+      w = cmul<T>(tj, w);
+      if (lane == 0) B(j, q) = csub<T>(B(j, q), w);
+      for (int i = j + 1 + lane; i < rows; i += 32) B(i, q) = csub<T>(B(i, q), cmul<T>(vcol[i], w));
+    }
+    __syncthreads();
+  }
+  if (SMEM) {
+    for (int64_t idx = tid; idx < (int64_t)rows * nq; idx += blockDim.x) {
+      const int i = (int)(idx / nq), q = (int)(idx % nq);
+      Bg[(int64_t)i * ldq + q] = Bs[(int64_t)q * rows + i];
+    }
+  }
+}
+}  // namespace
+
+template <typename T>
+void qr_factor_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const View<T> &in, cx<T> *vws,
+                      cx<T> *tau, cx<T> *rstack) {
+  const size_t bytes = (size_t)mc * n * sizeof(cx<T>);
+  if (bytes <= SMEM_CAP) {
+    cudaFuncSetAttribute(k_qr_factor<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    k_qr_factor<T, true><<<nchunks, QR_NT, bytes, st>>>(m, n, mc, in, vws, tau, rstack);
+  } else {
+    k_qr_factor<T, false><<<nchunks, QR_NT, 0, st>>>(m, n, mc, in, vws, tau, rstack);
+  }
+  count_launch();
+}
+
+template <typename T>
+void qr_apply_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const cx<T> *vws, const cx<T> *tau,
+                     const cx<T> *bin, int64_t ldb, int nq, cx<T> *qout, int64_t ldq) {
+  const size_t bytes = ((size_t)mc + (size_t)mc * nq) * sizeof(cx<T>);
+  if (bytes <= SMEM_CAP) {
+    cudaFuncSetAttribute(k_qr_apply<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    k_qr_apply<T, true><<<nchunks, QR_NT, bytes, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
+  } else {
+    const size_t vb = (size_t)mc * sizeof(cx<T>);
+    cudaFuncSetAttribute(k_qr_apply<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vb);
+    k_qr_apply<T, false><<<nchunks, QR_NT, vb, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
+  }
+  count_launch();
+}
+
+template void qr_factor_chunks<float>(cudaStream_t, int, int, int, int, const View<float> &, cx<float> *,
+                                      cx<float> *, cx<float> *);
+template void qr_factor_chunks<double>(cudaStream_t, int, int, int, int, const View<double> &, cx<double> *,
+                                       cx<double> *, cx<double> *);
+template void qr_apply_chunks<float>(cudaStream_t, int, int, int, int, const cx<float> *, const cx<float> *,
+                                     const cx<float> *, int64_t, int, cx<float> *, int64_t);
+template void qr_apply_chunks<double>(cudaStream_t, int, int, int, int, const cx<double> *,
+                                      const cx<double> *, const cx<double> *, int64_t, int, cx<double> *,
+                                      int64_t);
+
+}  // namespace mpdo

@@ -1,0 +1,206 @@
+"""Python handle over the C ABI: one ``Engine`` per device, ``Chain`` objects
+holding an MPDO on that device.  Arrays cross the boundary as host numpy
+buffers (complex values as interleaved float64)."""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, load
+
+_engines: Dict[int, 'Engine'] = {}
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _cplx(a) -> np.ndarray:
+    """complex array -> contiguous interleaved float64 view."""
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.complex128))
+    return a.view(np.float64)
+
+
+class Engine:
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = C.c_void_p()
+        check(self._lib.mpdo_engine_create(int(device), C.byref(h)))
+        self.handle = h
+        self.device = int(device)
+
+    @classmethod
+    def get(cls, device: int = 0) -> 'Engine':
+        if device not in _engines:
+            _engines[device] = cls(device)
+        return _engines[device]
+
+    def set_option(self, name: str, value: float) -> None:
+        check(self._lib.mpdo_engine_set_option(self.handle, name.encode(), float(value)))
+
+    def sync(self) -> None:
+        check(self._lib.mpdo_engine_sync(self.handle))
+
+    def set_stream(self, stream_ptr: Optional[int]) -> None:
+        check(self._lib.mpdo_engine_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
+
+    def debug_qr(self, a, dtype: str = 'complex128'):
+        """Kernel test hook: Householder QR of a host matrix on the GPU."""
+        a = np.asarray(a, dtype=np.complex128)
+        m, n = a.shape
+        k = min(m, n)
+        q = np.zeros(2 * m * k)
+        r = np.zeros(2 * k * n)
+        check(self._lib.mpdo_debug_qr(self.handle, _lib.MPDO_C128 if dtype.endswith('128') else _lib.MPDO_C64,
+                                      m, n, _dptr(_cplx(a)), _dptr(q), _dptr(r)))
+        return q.view(np.complex128).reshape(m, k), r.view(np.complex128).reshape(k, n)
+
+    def debug_svd(self, a, dtype: str = 'complex128'):
+        """Kernel test hook: right singular vectors (QR + one-sided Jacobi)."""
+        a = np.asarray(a, dtype=np.complex128)
+        m, n = a.shape
+        w = np.zeros(2 * n * n)
+        s = np.zeros(n)
+        check(self._lib.mpdo_debug_svd(self.handle, _lib.MPDO_C128 if dtype.endswith('128') else _lib.MPDO_C64,
+                                       m, n, _dptr(_cplx(a)), _dptr(w), _dptr(s)))
+        return w.view(np.complex128).reshape(n, n).T, s
+
+    def debug_split(self, y, keep: int, dtype: str = 'complex128'):
+        """Kernel test hook: Y ~= L R with L = U sqrt(S), R = sqrt(S) V^H (top keep)."""
+        y = np.asarray(y, dtype=np.complex128)
+        m, n = y.shape
+        lo = np.zeros(2 * m * keep)
+        ro = np.zeros(2 * keep * n)
+        check(self._lib.mpdo_debug_split(self.handle, _lib.MPDO_C128 if dtype.endswith('128') else _lib.MPDO_C64,
+                                         m, n, int(keep), _dptr(_cplx(y)), _dptr(lo), _dptr(ro)))
+        return lo.view(np.complex128).reshape(m, keep), ro.view(np.complex128).reshape(keep, n)
+
+    def launch_count(self) -> int:
+        c = C.c_uint64()
+        check(self._lib.mpdo_engine_launch_count(self.handle, C.byref(c)))
+        return int(c.value)
+
+
+class Chain:
+    """An MPDO on the GPU (site tensors A[l][s][a][r])."""
+
+    def __init__(self, vectors, dtype: str = 'complex64', connected: bool = False,
+                 engine: Optional[Engine] = None, _handle=None):
+        self.engine = engine or Engine.get(0)
+        self._lib = self.engine._lib
+        self.dtype = 'complex128' if str(dtype).endswith('128') else 'complex64'
+        if _handle is not None:
+            self.handle = _handle
+        else:
+            v = _cplx(np.asarray(vectors, dtype=np.complex128).reshape(-1, 2))
+            h = C.c_void_p()
+            check(self._lib.mpdo_chain_create(self.engine.handle, v.size // 4,
+                                              _lib.MPDO_C128 if self.dtype == 'complex128' else _lib.MPDO_C64,
+                                              _dptr(v), int(bool(connected)), C.byref(h)))
+            self.handle = h
+        n = C.c_int()
+        check(self._lib.mpdo_chain_num_sites(self.handle, C.byref(n)))
+        self.n = n.value
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h is not None and h.value:
+            try:
+                self._lib.mpdo_chain_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def clone(self) -> 'Chain':
+        h = C.c_void_p()
+        check(self._lib.mpdo_chain_clone(self.handle, C.byref(h)))
+        return Chain(None, self.dtype, engine=self.engine, _handle=h)
+
+    # ---- gates ------------------------------------------------------------
+    def apply_1q(self, site: int, kraus) -> None:
+        k = np.asarray(kraus, dtype=np.complex128)
+        if k.ndim == 2:
+            k = k[:, :, None]
+        buf = _cplx(k)
+        check(self._lib.mpdo_apply_1q(self.handle, int(site), _dptr(buf), int(k.shape[-1])))
+
+    def apply_2q(self, site_min: int, kraus, cutoff: float) -> None:
+        k = np.asarray(kraus, dtype=np.complex128)
+        if k.ndim == 4:
+            k = k[..., None]
+        buf = _cplx(k)
+        check(self._lib.mpdo_apply_2q(self.handle, int(site_min), _dptr(buf), int(k.shape[-1]), float(cutoff)))
+
+    def truncate(self, chi: Optional[int], kappa: Optional[int], max_err: Optional[float], noisy: bool,
+                 report: bool = False):
+        out = np.zeros(max(self.n - 1, 1), dtype=np.float64) if report else None
+        check(self._lib.mpdo_truncate(self.handle, int(chi or 0), int(kappa or 0),
+                                      -1.0 if max_err is None else float(max_err), int(bool(noisy)),
+                                      _dptr(out) if report else None))
+        return out[: self.n - 1] if report else None
+
+    def kappa_truncate(self, kappa: Optional[int], max_err: Optional[float]) -> None:
+        check(self._lib.mpdo_kappa_truncate(self.handle, int(kappa or 0),
+                                            -1.0 if max_err is None else float(max_err)))
+
+    # ---- inspection -------------------------------------------------------
+    def site_dims(self, site: int):
+        d = (C.c_int * 4)()
+        check(self._lib.mpdo_chain_site_dims(self.handle, int(site), d))
+        return tuple(d)
+
+    def dims(self):
+        return [self.site_dims(i) for i in range(self.n)]
+
+    def bond_present(self, bond: int) -> bool:
+        p = C.c_int()
+        check(self._lib.mpdo_chain_bond_present(self.handle, int(bond), C.byref(p)))
+        return bool(p.value)
+
+    def site(self, i: int) -> np.ndarray:
+        d = self.site_dims(i)
+        out = np.zeros(int(np.prod(d)) * 2, dtype=np.float64)
+        check(self._lib.mpdo_chain_read_site(self.handle, int(i), _dptr(out)))
+        return out.view(np.complex128).reshape(d)
+
+    def write_site(self, i: int, tensor) -> None:
+        t = np.asarray(tensor, dtype=np.complex128)
+        d = (C.c_int * 4)(*t.shape)
+        buf = _cplx(t)
+        check(self._lib.mpdo_chain_write_site(self.handle, int(i), d, _dptr(buf)))
+
+    # ---- readout ----------------------------------------------------------
+    def reduced_dm(self, keep: Optional[Sequence[int]] = None) -> np.ndarray:
+        keep = list(range(self.n)) if keep is None else sorted(int(q) for q in keep)
+        m = len(keep)
+        arr = (C.c_int * max(m, 1))(*keep)
+        out = np.zeros(2 * 4 ** m, dtype=np.float64)
+        check(self._lib.mpdo_reduced_dm(self.handle, arr, m, _dptr(out)))
+        return out.view(np.complex128).reshape(2 ** m, 2 ** m)
+
+    def probs(self, keep: Optional[Sequence[int]] = None) -> np.ndarray:
+        keep = list(range(self.n)) if keep is None else sorted(int(q) for q in keep)
+        m = len(keep)
+        arr = (C.c_int * max(m, 1))(*keep)
+        out = np.zeros(2 ** m, dtype=np.float64)
+        check(self._lib.mpdo_probs(self.handle, arr, m, _dptr(out)))
+        return out
+
+    def expect_ops(self, ops: Dict[int, np.ndarray]) -> float:
+        sites = sorted(ops)
+        arr = (C.c_int * max(len(sites), 1))(*sites)
+        buf = _cplx(np.stack([np.asarray(ops[q], dtype=np.complex128).reshape(2, 2) for q in sites])
+                    if sites else np.zeros((1, 2, 2)))
+        out = C.c_double()
+        check(self._lib.mpdo_expect_ops(self.handle, arr, _dptr(buf), len(sites), C.byref(out)))
+        return float(out.value)
+
+    def expect_pauli_batch(self, codes) -> np.ndarray:
+        codes = np.ascontiguousarray(np.asarray(codes, dtype=np.int8).reshape(-1, self.n))
+        out = np.zeros(codes.shape[0], dtype=np.float64)
+        check(self._lib.mpdo_expect_pauli_batch(self.handle, codes.ctypes.data_as(C.POINTER(C.c_int8)),
+                                                codes.shape[0], _dptr(out)))
+        return out
