@@ -75,6 +75,14 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
 /* Wait for all queued work; returns the first deferred device status
  * (NOT_CONVERGED / NONFINITE) raised since the last sync. */
 mpdo_status mpdo_engine_sync(mpdo_engine_t eng);
+/* Per-kernel-class timing (no counterpart in the reference).  While enabled,
+ * every launch is bracketed by CUDA events on the engine stream and its
+ * algorithmic flop and byte counts are accumulated.  Classes: 0 GEMM,
+ * 1 Householder QR factor, 2 QR explicit-Q apply, 3 one-sided Jacobi,
+ * 4 Kraus 1q apply, 5 two-site gate mix, 6 other.  Enabling resets the sums. */
+mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable);
+mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *launches, double *ms,
+                                     double *flops, double *bytes);
 /* Number of kernels this engine launched so far. */
 mpdo_status mpdo_engine_launch_count(mpdo_engine_t eng, uint64_t *count);
 

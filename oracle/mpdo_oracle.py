@@ -286,14 +286,26 @@ def randomized_svd(M: torch.Tensor, n_components: int, n_oversamples: int = 7):
     return q @ u, s, vh
 
 
+_AARCH64 = __import__('platform').machine() in ('aarch64', 'arm64')
+
+
+def _svd128(M: torch.Tensor):
+    if _AARCH64:
+        # the divide-and-conquer SVD of the Arm hosts' LAPACK aborts the whole
+        # process (xerbla) on some inputs; the QR-iteration driver does not
+        import scipy.linalg
+        u, s, vh = scipy.linalg.svd(M.numpy(), full_matrices=False, lapack_driver='gesvd')
+        return torch.from_numpy(u), torch.from_numpy(s), torch.from_numpy(vh)
+    return torch.linalg.svd(M, full_matrices=False)
+
+
 def _svd(M: torch.Tensor):
     """Thin SVD.  complex64 inputs are factorised in complex128 and the factors
-    rounded back to complex64: the state keeps fp32 storage, and the Arm hosts'
-    LAPACK (which aborts the process on some complex64 SVDs) is not used."""
+    rounded back to complex64 (the state keeps fp32 storage)."""
     if M.dtype == torch.complex64:
-        u, s, vh = torch.linalg.svd(M.to(torch.complex128), full_matrices=False)
+        u, s, vh = _svd128(M.to(torch.complex128))
         return u.to(torch.complex64), s.to(torch.float32), vh.to(torch.complex64)
-    return torch.linalg.svd(M, full_matrices=False)
+    return _svd128(M)
 
 
 def _qr(M: torch.Tensor):
@@ -590,3 +602,74 @@ def density2prob(rho: torch.Tensor) -> np.ndarray:
 def trace(st: MPDO) -> float:
     """dmOperations.py:40-48."""
     return float(expect_ops(st, {}))
+
+
+# ----------------------------------------------------------------------------
+# timed CPU baseline: one layer of a circuit with a time budget
+# ----------------------------------------------------------------------------
+def time_layer(st: MPDO, layer_ops, chi, kappa, max_err=None, noisy=True, budget_s: float = 20.0):
+    """Run one layer (its gate sublayers and truncates) on the CPU and return
+    the estimated wall time of the whole layer.  Gate applications, QR sweeps
+    and kappa passes run in full; SVD right-to-left sweeps run until the budget
+    is spent and the remaining steps are extrapolated from the mean measured
+    step time of the same bond kind (even / odd bond).  Returns
+    (seconds, dict(measured=..., extrapolated_steps=...))."""
+    import time
+    t_total = 0.0
+    extrap_steps = 0
+    measured_steps = 0
+    t_start = time.perf_counter()
+    for op in layer_ops:
+        if op[0] != 'truncate':
+            t0 = time.perf_counter()
+            if op[0] == '1q':
+                apply_1q(st, op[1], op[2])
+            else:
+                i, t = orient_2q(op[1], op[2], op[3])
+                apply_2q(st, i, t)
+            t_total += time.perf_counter() - t0
+            continue
+        if not connected(st):
+            continue
+        t0 = time.perf_counter()
+        qr_left2right(st)
+        t_total += time.perf_counter() - t0
+        step_t = {0: [], 1: []}
+        for idx in range(st.n - 1, 0, -1):
+            kind = idx % 2
+            if time.perf_counter() - t_start > budget_s and step_t[kind]:
+                t_total += sum(step_t[kind]) / len(step_t[kind])
+                extrap_steps += 1
+                # keep the shapes of the truncated sites (values are no longer
+                # used for anything but timing)
+                a, b = st.sites[idx - 1], st.sites[idx]
+                k = min(chi or 10 ** 9, a.shape[0] * 2 * a.shape[2], 2 * b.shape[2] * b.shape[3])
+                # (no exact-zero blocks: some LAPACK builds abort the process
+                # on all-zero inputs)
+                g = torch.Generator().manual_seed(idx)
+                a2 = 1e-3 * torch.randn(a.shape[:3] + (k,), dtype=a.dtype, generator=g)
+                b2 = 1e-3 * torch.randn((k,) + b.shape[1:], dtype=b.dtype, generator=g)
+                kk = min(k, a.shape[3])
+                a2[..., :kk] = a[..., :kk]
+                b2[:kk] = b[:kk]
+                st.sites[idx - 1], st.sites[idx] = a2, b2
+                continue
+            t0 = time.perf_counter()
+            a, b = st.sites[idx - 1], st.sites[idx]
+            l, x, aa, _ = a.shape
+            _, y, cc, r = b.shape
+            m = torch.einsum('lsam,mtcr->lsatcr', a, b).reshape(l * x * aa, y * cc * r)
+            u, s, vh, _ = svd_truncate(m, chi, max_err, relative=True)
+            ss = torch.sqrt(s).to(m.dtype)
+            k = s.numel()
+            st.sites[idx - 1] = (u * ss[None, :]).reshape(l, x, aa, k)
+            st.sites[idx] = (ss[:, None] * vh).reshape(k, y, cc, r)
+            dt = time.perf_counter() - t0
+            step_t[kind].append(dt)
+            t_total += dt
+            measured_steps += 1
+        if noisy:
+            t0 = time.perf_counter()
+            svd_kappa(st, kappa, max_err)
+            t_total += time.perf_counter() - t0
+    return t_total, dict(measured_svd_steps=measured_steps, extrapolated_svd_steps=extrap_steps)

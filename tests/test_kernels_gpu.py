@@ -86,3 +86,16 @@ def test_qr_columns_near_underflow(eng, dtype, scale, tol):
     assert np.abs(q @ r - a).max() <= tol * np.abs(a).max() * 4
     w, s = eng.debug_svd(a, dtype)
     assert np.isfinite(w).all() and np.abs(w.conj().T @ w - np.eye(64)).max() <= tol * 10
+
+
+@pytest.mark.parametrize('m,n,keep,rank', [(128, 2048, 128, 20), (256, 8192, 64, 40), (200, 300, 150, 7)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-4)])
+def test_split_wide_rank_deficient(eng, m, n, keep, rank, dtype, tol):
+    # wide bonds go through the Gram / block-Jacobi / Rayleigh-Ritz path; exact
+    # rank deficiency must not break the orthonormality of the basis
+    y = _rand(m, n, 11 * m + n, rank)
+    L, R = eng.debug_split(y, keep, dtype)
+    u, s, vh = np.linalg.svd(y, full_matrices=False)
+    k = min(keep, len(s))
+    best = (u[:, :k] * s[:k]) @ vh[:k]
+    np.testing.assert_allclose(L @ R, best, atol=tol * s[0] * 10)

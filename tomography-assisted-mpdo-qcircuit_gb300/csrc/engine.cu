@@ -54,7 +54,44 @@ struct Engine {
   bool fuse_2q = true;
   int max_sweeps = 60;
   int first_status = 0;
+  // per-kernel-class profiling (CUDA events around each launch)
+  struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };
+  bool profiling = false;
+  std::vector<ProfRec> recs;
+  double acc_ms[8] = {0}, acc_flops[8] = {0}, acc_bytes[8] = {0};
+  long long acc_n[8] = {0};
 };
+
+// kernel classes reported by mpdo_engine_profile_read
+enum KClass { K_GEMM = 0, K_QR_FACTOR = 1, K_QR_APPLY = 2, K_JACOBI = 3, K_KRAUS1Q = 4, K_MIX2Q = 5, K_OTHER = 6 };
+
+// Launch wrapper: when profiling, bracket the launch with events and keep the
+// algorithmic flop/byte count of the call.
+template <class F> static void prof(Engine &e, int cls, double flops, double bytes, F &&launch) {
+  if (!e.profiling) { launch(); return; }
+  Engine::ProfRec r{cls, nullptr, nullptr, flops, bytes};
+  cudaEventCreate(&r.a);
+  cudaEventCreate(&r.b);
+  cudaEventRecord(r.a, e.stream);
+  launch();
+  cudaEventRecord(r.b, e.stream);
+  e.recs.push_back(r);
+}
+static void prof_flush(Engine &e) {
+  if (e.recs.empty()) return;
+  cudaStreamSynchronize(e.stream);
+  for (auto &r : e.recs) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    e.acc_ms[r.cls] += ms;
+    e.acc_flops[r.cls] += r.flops;
+    e.acc_bytes[r.cls] += r.bytes;
+    e.acc_n[r.cls] += 1;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  e.recs.clear();
+}
 
 static void *dalloc(Engine &e, size_t bytes) {
   if (bytes == 0) bytes = 16;
@@ -132,18 +169,22 @@ template <typename T> static View<T> CM(const cx<T> *p, int64_t ld, int conj = 0
 template <typename T>
 static void gemm(Engine &e, int M, int N, int K, const View<T> &A, const View<T> &B, cx<T> *C, int64_t ldc,
                  int batch = 1, int64_t cbs = 0, cx<T> beta = czero<T>()) {
-  // split-K workspace for small-output long-K products (Gram matrices)
+  const double fl = 8.0 * M * N * K * batch;
+  const double by = (double)sizeof(cx<T>) * batch * ((double)M * K + (double)K * N + (double)M * N);
+  // split-K workspace for small-output long-K products
   const int64_t tiles = (int64_t)((M + 63) / 64) * ((N + 63) / 64) * batch;
   if (K >= 512 && tiles < 148) {
     const int nsplit = (int)std::min<int64_t>(std::max<int64_t>(1, 296 / tiles), K / 128);
     if (nsplit > 1) {
       const size_t ws = (size_t)nsplit * batch * M * N;
       DBuf<cx<T>> w(e, ws);
-      cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs, w.p, ws);
+      prof(e, K_GEMM, fl, by, [&] {
+        cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs, w.p, ws);
+      });
       return;
     }
   }
-  cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs);
+  prof(e, K_GEMM, fl, by, [&] { cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs); });
 }
 
 template <typename T> static cx<T> *site_ptr(mpdo_chain_s *ch, int i) { return static_cast<cx<T> *>(ch->s[i].p); }
@@ -171,24 +212,33 @@ static void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
   View<T> cur = in;
   int curm = m;
   while (true) {
+    // chunk rows: the whole matrix if it fits in shared memory, else the
+    // largest multiple of 32 that fits (with the explicit-Q pass) and exceeds
+    // n, so that every level shrinks the stacked R; else one global chunk
     int mc;
     if ((size_t)curm * n * esz <= cap) mc = curm;
-    else if (n <= 128 && (size_t)curm >= 4 * (size_t)n) {
+    else {
       size_t mcs = cap / ((size_t)(n + 1) * esz);
       mcs = mcs / 32 * 32;
-      if (mcs < 2 * (size_t)n) mc = curm; else mc = (int)std::min<size_t>(mcs, (size_t)curm);
-    } else mc = curm;
+      mc = (mcs > (size_t)n) ? (int)std::min<size_t>(mcs, (size_t)curm) : curm;
+    }
     const int nch = (curm + mc - 1) / mc;
     Level L;
     L.m = curm; L.mc = mc; L.nch = nch;
     L.v = DBuf<cx<T>>(e, (size_t)nch * mc * n);
     L.tau = DBuf<cx<T>>(e, (size_t)nch * n);
     L.rs = DBuf<cx<T>>(e, (size_t)nch * n * n);
-    qr_factor_chunks<T>(e.stream, curm, n, mc, nch, cur, L.v.p, L.tau.p, L.rs.p);
+    {
+      const double mm = (double)std::min(mc, curm), nn = n, kk = std::min(mm, nn);
+      const double fl = nch * 4.0 * (2.0 * mm * nn * kk - (mm + nn) * kk * kk + 2.0 / 3.0 * kk * kk * kk);
+      const double by = (double)sizeof(cx<T>) * ((double)curm * n + (double)nch * n * n);
+      prof(e, K_QR_FACTOR, fl, by, [&] { qr_factor_chunks<T>(e.stream, curm, n, mc, nch, cur, L.v.p, L.tau.p, L.rs.p); });
+    }
     lv.push_back(std::move(L));
     if (nch == 1) break;
+    // compact stack: full chunks give n rows each, the last min(rows, n)
     cur = RM<T>(lv.back().rs.p, n);
-    curm = nch * n;
+    curm = (nch - 1) * n + std::min(n, curm - (nch - 1) * mc);
   }
   const int k = std::min(m, n);
   const Level &top = lv.back();
@@ -208,7 +258,12 @@ static void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
       out = nb.p;
       if (li % 2) { qa = std::move(nb); } else { qb = std::move(nb); }
     }
-    qr_apply_chunks<T>(e.stream, L.m, n, L.mc, L.nch, L.v.p, L.tau.p, bin, k, k, out, k);
+    {
+      const double mm = (double)std::min(L.mc, L.m), kk = std::min<double>(mm, n);
+      const double fl = L.nch * 4.0 * (4.0 * mm * k * kk - 2.0 * k * kk * kk);
+      const double by = (double)sizeof(cx<T>) * ((double)L.m * n + (double)L.m * k);
+      prof(e, K_QR_APPLY, fl, by, [&] { qr_apply_chunks<T>(e.stream, L.m, n, L.mc, L.nch, L.v.p, L.tau.p, bin, k, k, out, k); });
+    }
     bin = out;
   }
 }
@@ -227,8 +282,107 @@ static void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W
   W = DBuf<cx<T>>(e, (size_t)n * n);
   sigma = DBuf<T>(e, n);
   DBuf<cx<T>> U(e, (size_t)k * n), xws(e, (size_t)k * n), wws(e, (size_t)n * n);
-  jacobi_svd<T>(e.stream, 1, k, n, RM<T>(R.p, n), U.p, sigma.p, W.p, xws.p, wws.p, e.max_sweeps,
-                status_slot(e, 1));
+  {
+    // algorithmic count of a thin SVD of the k x n factor with vectors
+    const double mm = std::max(k, n), nn = std::min(k, n);
+    const double fl = 4.0 * (4.0 * mm * nn * nn + 22.0 * nn * nn * nn);
+    const double by = (double)sizeof(cx<T>) * ((double)k * n * 2 + (double)n * n);
+    int *slot = status_slot(e, 1);
+    prof(e, K_JACOBI, fl, by, [&] {
+      jacobi_svd<T>(e.stream, 1, k, n, RM<T>(R.p, n), U.p, sigma.p, W.p, xws.p, wws.p, e.max_sweeps, slot);
+    });
+  }
+}
+
+// --------------------------------------------------- wide-bond SVD ----
+// One-sided block Jacobi on the columns of X (m x n, column-major, in place):
+// tournament ordering over column blocks, one CTA per block pair per round,
+// repeated until an outer sweep makes no rotation.
+template <typename T>
+static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
+  const size_t esz = sizeof(cx<T>), cap = 200 * 1024;
+  int bs = (int)std::min<size_t>(cap / (2 * (size_t)m * esz), 32);
+  bs = std::max(4, std::min(bs, std::max(8, n / 16)));
+  const int nblk = (n + bs - 1) / bs;
+  const int nb = nblk + (nblk & 1);
+  const int rounds = nb - 1, np = nb / 2;
+  std::vector<int> pairs((size_t)rounds * np * 2);
+  for (int r = 0; r < rounds; ++r)
+    for (int p = 0; p < np; ++p) {
+      int a, c;
+      if (p == 0) { a = nb - 1; c = r; }
+      else { a = (r + p) % (nb - 1); c = (r - p + nb - 1) % (nb - 1); }
+      pairs[((size_t)r * np + p) * 2] = a;
+      pairs[((size_t)r * np + p) * 2 + 1] = c;
+    }
+  DBuf<int> dp(e, pairs.size()), flag(e, 1);
+  DBuf<T> gmax(e, 1);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(dp.p, pairs.data(), pairs.size() * sizeof(int), cudaMemcpyHostToDevice, e.stream));
+  colmax2<T>(e.stream, m, n, X, gmax.p);
+  int hflag = 1;
+  for (int outer = 0; outer < 40 && hflag; ++outer) {
+    MPDO_CUDA_CHECK(cudaMemsetAsync(flag.p, 0, sizeof(int), e.stream));
+    const double fl = 4.0 * (4.0 * m * (double)n * n) / std::max(1, rounds);
+    for (int r = 0; r < rounds; ++r)
+      prof(e, K_JACOBI, fl, (double)esz * m * n * 2, [&] {
+        bjacobi_round<T>(e.stream, m, n, bs, nblk, X, dp.p + (size_t)r * np * 2, np, gmax.p, 2, flag.p);
+      });
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  }
+}
+
+// Leading left singular vectors of a wide-bond Y (Mr x Nc): eigenvectors of
+// the Gram matrix Y Y^H by block Jacobi, then a Rayleigh-Ritz refinement in
+// the leading kr = min(Mr, want + 16) directions (QR + one-sided Jacobi of
+// Z = U^H Y), which restores the accuracy of the small singular values.
+// U: Mr x kr column-major; s: Mr values (kr refined, the rest from the Gram).
+template <typename T>
+static void left_svd_wide(Engine &e, const cx<T> *Y, int Mr, int Nc, int want, DBuf<cx<T>> &U, DBuf<T> &s,
+                          int &kr) {
+  DBuf<cx<T>> G(e, (size_t)Mr * Mr), X(e, (size_t)Mr * Mr);
+  gemm<T>(e, Mr, Mr, Nc, RM<T>(Y, Nc), CM<T>(Y, Nc, 1), G.p, Mr);
+  {  // X (column-major) = G^T = conj(G) for a Hermitian G stored row-major
+    const int64_t d[4] = {1, 1, 1, (int64_t)Mr * Mr};
+    const int64_t st[4] = {0, 0, 0, 1};
+    copy4d<T>(e.stream, X.p, G.p, d, st, 1);
+  }
+  G.reset();
+  block_jacobi<T>(e, Mr, Mr, X.p);
+  DBuf<cx<T>> Ua(e, (size_t)Mr * Mr), xws(e, (size_t)Mr * Mr);
+  DBuf<T> lam(e, Mr);
+  jacobi_svd<T>(e.stream, 1, Mr, Mr, CM<T>(X.p, Mr), Ua.p, lam.p, nullptr, xws.p, nullptr, 0, status_slot(e, 1));
+  X.reset();
+  xws.reset();
+  kr = std::min(Mr, want + 16);
+  // Orthonormal basis of the leading kr eigenvector columns: directions with
+  // rounding-level eigenvalues come out of the normalisation as arbitrary,
+  // non-orthogonal vectors; Householder QR keeps the leading span and replaces
+  // them by an orthonormal completion.
+  DBuf<cx<T>> Qb(e, (size_t)Mr * kr), Rb(e, (size_t)kr * kr);
+  qr<T>(e, Mr, kr, CM<T>(Ua.p, Mr), Qb.p, Rb.p);                // Qb row-major Mr x kr
+  Ua.reset();
+  Rb.reset();
+  DBuf<cx<T>> Z(e, (size_t)kr * Nc);
+  gemm<T>(e, kr, Nc, Mr, CM<T>(Qb.p, kr, 1), RM<T>(Y, Nc), Z.p, Nc);   // Qb^H Y
+  DBuf<cx<T>> Wz;
+  DBuf<T> sz;
+  right_svd<T>(e, Nc, kr, CM<T>(Z.p, Nc, 1), Wz, sz);          // left singular vectors of Z
+  U = DBuf<cx<T>>(e, (size_t)Mr * kr);
+  gemm<T>(e, Mr, kr, kr, RM<T>(Qb.p, kr), CM<T>(Wz.p, kr), U.p, kr);   // row-major Mr x kr
+  {  // to column-major
+    DBuf<cx<T>> Uc(e, (size_t)Mr * kr);
+    const int64_t d[4] = {1, 1, kr, Mr};
+    const int64_t st[4] = {0, 0, 1, kr};
+    copy4d<T>(e.stream, Uc.p, U.p, d, st, 0);
+    U = std::move(Uc);
+  }
+  s = DBuf<T>(e, Mr);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p, sz.p, kr * sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
+  if (Mr > kr) {
+    sqrt_inplace<T>(e.stream, lam.p, Mr);
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p + kr, lam.p + kr, (Mr - kr) * sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
+  }
 }
 
 // --------------------------------------------------------- SVD split ----
@@ -241,15 +395,23 @@ static void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W
 // wsum (nullable): device double[2] = {kept, total} sum s^2.
 template <typename T, typename KeepFn>
 static void svd_split(Engine &e, const cx<T> *Y, int Mr, int Nc, KeepFn keep_fn, DBuf<cx<T>> &Lout,
-                      DBuf<cx<T>> &Rout, int &keep_out, double *wsum) {
+                      DBuf<cx<T>> &Rout, int &keep_out, double *wsum, int want = -1) {
   DBuf<cx<T>> W;
   DBuf<T> sg;
-  right_svd<T>(e, Nc, Mr, CM<T>(Y, Nc, 1), W, sg);       // view of Y^H (Nc x Mr)
   const int nsv_ref = std::min(Mr, Nc);
-  const int keep = keep_fn(sg.p, nsv_ref);
+  const size_t esz = sizeof(cx<T>);
+  int kr = Mr;   // number of computed singular vectors
+  if (2 * (size_t)Mr * Mr * esz <= 200 * 1024) {
+    right_svd<T>(e, Nc, Mr, CM<T>(Y, Nc, 1), W, sg);       // view of Y^H (Nc x Mr)
+  } else {
+    left_svd_wide<T>(e, Y, Mr, Nc, want < 0 ? nsv_ref : std::min(want, nsv_ref), W, sg, kr);
+  }
+  int keep = keep_fn(sg.p, nsv_ref);
+  if (std::min(keep, nsv_ref) > kr) fail(MPDO_ERR_BAD_SHAPE, "internal: kept more vectors than refined");
   keep_out = keep;
   if (wsum) sigma_weights<T>(e.stream, sg.p, Mr, keep, wsum);
   const int kk = std::min(keep, nsv_ref);
+  (void)kr;
   Lout = DBuf<cx<T>>(e, (size_t)Mr * std::max(keep, 1));
   Rout = DBuf<cx<T>>(e, (size_t)std::max(keep, 1) * Nc);
   if (keep > kk) {
@@ -315,7 +477,8 @@ template <typename T> static void apply_1q(mpdo_chain_s *ch, int site, const dou
   materialize_touching<T>(ch, site);
   const Site s = ch->s[site];
   DBuf<cx<T>> out(e, (size_t)s.l * 2 * s.a * K * s.r);
-  kraus1q<T>(e.stream, site_ptr<T>(ch, site), out.p, s.l, s.a, s.r, kraus, K);
+  prof(e, K_KRAUS1Q, 8.0 * 2 * 2 * K * s.elems(), (double)sizeof(cx<T>) * s.elems() * (1 + K),
+       [&] { kraus1q<T>(e.stream, site_ptr<T>(ch, site), out.p, s.l, s.a, s.r, kraus, K); });
   set_site<T>(ch, site, out.release(), s.l, s.a * K, s.r);
 }
 
@@ -406,7 +569,8 @@ template <typename T> static void qr_sweep(mpdo_chain_s *ch) {
       gemm<T>(e, kq, ncol, m, View<T>{Rp.p, (int64_t)m, 1, nc, 0, 1, 0}, RM<T>(site_ptr<T>(ch, i + 1), ncol), W.p,
               ncol, 2, (int64_t)kq * ncol);
       DBuf<cx<T>> Z(e, (size_t)2 * kq * 2 * c * K * r);
-      mix2q<T>(e.stream, W.p, Z.p, kq, c, r, pd.t.data(), K);
+      prof(e, K_MIX2Q, 8.0 * 16 * K * (double)kq * c * r, (double)sizeof(cx<T>) * 4.0 * kq * c * r * (1 + K),
+           [&] { mix2q<T>(e.stream, W.p, Z.p, kq, c, r, pd.t.data(), K); });
       set_site<T>(ch, i + 1, Z.release(), 2 * kq, c * K, r);
       continue;
     }
@@ -449,7 +613,9 @@ template <typename T> static void svd_sweep(mpdo_chain_s *ch, int chi, double ma
     };
     DBuf<cx<T>> Lf, Rf;
     int keep = 0;
-    svd_split<T>(e, site_ptr<T>(ch, idx), b, Nc, keep_fn, Lf, Rf, keep, wdev ? wdev + 2 * (idx - 1) : nullptr);
+    const int want = chi > 0 ? std::min(chi, std::min(rows_prev, Nc)) : -1;
+    svd_split<T>(e, site_ptr<T>(ch, idx), b, Nc, keep_fn, Lf, Rf, keep, wdev ? wdev + 2 * (idx - 1) : nullptr,
+                 max_err < 0 ? want : -1);
     DBuf<cx<T>> NP(e, (size_t)rows_prev * keep);
     gemm<T>(e, rows_prev, keep, b, RM<T>(site_ptr<T>(ch, idx - 1), b), RM<T>(Lf.p, keep), NP.p, keep);
     set_site<T>(ch, idx - 1, NP.release(), P.l, P.a, keep);
@@ -889,6 +1055,30 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
     if (k == "fuse_2q") e.fuse_2q = value != 0;
     else if (k == "max_sweeps") { need(value >= 1 && value <= 1000, "max_sweeps out of range"); e.max_sweeps = (int)value; }
     else fail(MPDO_ERR_INVALID, "unknown option: " + k);
+  });
+}
+
+mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable) {
+  return guard([&] {
+    need(eng != nullptr, "engine is NULL");
+    Engine &e = eng->e;
+    prof_flush(e);
+    for (int c = 0; c < 8; ++c) { e.acc_ms[c] = e.acc_flops[c] = e.acc_bytes[c] = 0; e.acc_n[c] = 0; }
+    e.profiling = enable != 0;
+  });
+}
+
+mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *launches, double *ms, double *flops,
+                                     double *bytes) {
+  return guard([&] {
+    need(eng && launches && ms && flops && bytes, "NULL argument");
+    need(kclass >= 0 && kclass < 8, "kernel class out of range");
+    Engine &e = eng->e;
+    prof_flush(e);
+    *launches = e.acc_n[kclass];
+    *ms = e.acc_ms[kclass];
+    *flops = e.acc_flops[kclass];
+    *bytes = e.acc_bytes[kclass];
   });
 }
 

@@ -38,12 +38,23 @@ void qr_apply_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const c
 // columns by Hestenes-Jacobi rotations: X W = U diag(sigma).  Outputs, sorted
 // by sigma descending: U (m x n column-major per batch in `uout`, zero columns
 // where sigma == 0), sigma (n per batch) and, when wout != nullptr, W
-// (n x n column-major per batch).  xws: workspace m x n per batch (may be
-// uout).  wws: workspace n x n per batch when W is wanted.  status[b] gets a
-// DevStatus.
+// (n x n column-major per batch).  xws: workspace m x n per batch (distinct
+// from uout).  wws: workspace n x n per batch when W is wanted.  status[b]
+// gets a DevStatus.  max_sweeps = 0 only normalises and sorts the columns.
 template <typename T>
 void jacobi_svd(cudaStream_t st, int batch, int m, int n, const View<T> &in, cx<T> *uout, T *sigma,
                 cx<T> *wout, cx<T> *xws, cx<T> *wws, int max_sweeps, int *status);
+
+// One tournament round of a one-sided block-Jacobi sweep on the columns of X
+// (m x n column-major, in place, bs-column blocks, nblk blocks; pairs_round:
+// npairs block-id pairs, ids >= nblk are empty).  Several CTAs, one per pair.
+// *flag |= 1 when any rotation happened.  gmax2: max squared column norm.
+template <typename T>
+void bjacobi_round(cudaStream_t st, int m, int n, int bs, int nblk, cx<T> *X, const int *pairs_round, int npairs,
+                   const T *gmax2, int inner_sweeps, int *flag);
+// *out = max_j |X[:, j]|^2 for an m x n column-major X
+template <typename T>
+void colmax2(cudaStream_t st, int m, int n, const cx<T> *X, T *out);
 
 // --------------------------------------------------- site-tensor kernels --
 // out[l][x][a*K+k][r] = sum_s G[x][s][k] A[l][s][a][r]     (K <= 16)

@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
   const int ne = n + (n & 1);
   const int npairs = ne / 2;
   int sweep = 0;
-  bool converged = (n < 2) || bad;
+  // max_sweeps == 0: the caller only wants the columns normalised and sorted
+  bool converged = (n < 2) || bad || max_sweeps == 0;
   __shared__ T colmax;
   const T floor_rel = T(16) * T(n) * Eps<T>::v * Eps<T>::v;
   for (; sweep < max_sweeps && !converged; ++sweep) {
@@ -166,6 +167,7 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
   __syncthreads();
   if (tid == 0 && status) status[b] = bad ? DEV_NONFINITE : (converged ? DEV_OK : DEV_NOT_CONVERGED);
 }
+
 }  // namespace
 
 template <typename T>
@@ -183,6 +185,136 @@ void jacobi_svd(cudaStream_t st, int batch, int m, int n, const View<T> &in, cx<
   }
   count_launch();
 }
+
+namespace {
+// ------------------------------------------------------ block Jacobi -----
+// One tournament round of a one-sided block-Jacobi sweep over the columns of X
+// (m x n, column-major in global memory).  CTA p loads the column blocks
+// pairs[2p], pairs[2p+1] (bs columns each; an id >= nblk is an empty block)
+// into shared memory, orthogonalises them against each other with up to
+// inner_sweeps one-sided Jacobi sweeps (no vector accumulation), writes them
+// back, and sets *flag when it rotated anything.  gmax2: the largest squared
+// column norm, for the rounding-level floor.
+template <typename T>
+__global__ void __launch_bounds__(512) k_bjacobi(int m, int n, int bs, int nblk, cx<T> *X, const int *pairs,
+                                                 T tol, const T *gmax2, int inner_sweeps, int *flag) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int rot_count, any_rot;
+  cx<T> *S = reinterpret_cast<cx<T> *>(smem_raw);
+  const int b0 = pairs[2 * blockIdx.x], b1 = pairs[2 * blockIdx.x + 1];
+  const int c0 = b0 * bs, c1 = b1 * bs;
+  const int w0 = (b0 < nblk) ? min(bs, n - c0) : 0;
+  const int w1 = (b1 < nblk) ? min(bs, n - c1) : 0;
+  const int nc = w0 + w1;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  if (tid == 0) any_rot = 0;
+  for (int64_t idx = tid; idx < (int64_t)m * nc; idx += blockDim.x) {
+    const int i = (int)(idx % m), j = (int)(idx / m);
+    const int col = j < w0 ? c0 + j : c1 + (j - w0);
+    S[(int64_t)j * m + i] = X[(int64_t)col * m + i];
+  }
+  __syncthreads();
+  const T floor_abs = (*gmax2) * T(16) * T(n) * Eps<T>::v * Eps<T>::v;
+  const int ne = nc + (nc & 1);
+  const int npairs = ne / 2;
+  for (int sw = 0; sw < inner_sweeps && nc >= 2; ++sw) {
+    if (tid == 0) rot_count = 0;
+    __syncthreads();
+    for (int r = 0; r < ne - 1; ++r) {
+      for (int p = warp; p < npairs; p += nw) {
+        int a, c;
+        if (p == 0) { a = ne - 1; c = r; }
+        else { a = (r + p) % (ne - 1); c = (r - p + ne - 1) % (ne - 1); }
+        if (a >= nc || c >= nc) continue;
+        // only pairs that straddle the two blocks need work after the first sweep
+        const int pc = min(a, c), qc = max(a, c);
+        cx<T> *xp = S + (int64_t)pc * m, *xq = S + (int64_t)qc * m;
+        T al = T(0), be = T(0);
+        cx<T> ga = czero<T>();
+        for (int i = lane; i < m; i += 32) {
+          const cx<T> u = xp[i], v = xq[i];
+          al += cabs2<T>(u);
+          be += cabs2<T>(v);
+          cfmac<T>(ga, u, v);
+        }
+        al = wsum(al); be = wsum(be); ga.x = wsum(ga.x); ga.y = wsum(ga.y);
+        const T g = sqrt(cabs2<T>(ga));
+        if (!(g > tol * sqrt(al * be)) || al <= floor_abs || be <= floor_abs || al <= Eps<T>::tiny ||
+            be <= Eps<T>::tiny || g <= Eps<T>::tiny)
+          continue;
+        const T zeta = (be - al) / (T(2) * g);
+        const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+        const T cs = T(1) / sqrt(T(1) + t * t);
+        const T sn = cs * t;
+        const cx<T> ec = cmk<T>(ga.x / g, -ga.y / g);
+        const cx<T> sec = cscale<T>(ec, sn), cec = cscale<T>(ec, cs);
+        for (int i = lane; i < m; i += 32) {
+          const cx<T> u = xp[i], v = xq[i];
+          const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
+          xp[i] = cmk<T>(cs * u.x - ev_s.x, cs * u.y - ev_s.y);
+          xq[i] = cmk<T>(sn * u.x + ev_c.x, sn * u.y + ev_c.y);
+        }
+        if (lane == 0) atomicAdd(&rot_count, 1);
+      }
+      __syncthreads();
+    }
+    const int rc = rot_count;
+    __syncthreads();
+    if (rc == 0) break;
+    if (tid == 0) any_rot = 1;
+  }
+  __syncthreads();
+  for (int64_t idx = tid; idx < (int64_t)m * nc; idx += blockDim.x) {
+    const int i = (int)(idx % m), j = (int)(idx / m);
+    const int col = j < w0 ? c0 + j : c1 + (j - w0);
+    X[(int64_t)col * m + i] = S[(int64_t)j * m + i];
+  }
+  if (tid == 0 && any_rot) atomicOr(flag, 1);
+}
+
+template <typename T>
+__global__ void k_colmax2(int m, int n, const cx<T> *X, T *out) {
+  __shared__ T red[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  T mx = T(0);
+  for (int j = warp; j < n; j += nw) {
+    T s = T(0);
+    for (int i = lane; i < m; i += 32) s += cabs2<T>(X[(int64_t)j * m + i]);
+    s = wsum(s);
+    mx = fmax(mx, s);
+  }
+  if (lane == 0) red[warp] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T v = T(0);
+    for (int w = 0; w < nw; ++w) v = fmax(v, red[w]);
+    *out = v;
+  }
+}
+}  // namespace
+
+template <typename T>
+void bjacobi_round(cudaStream_t st, int m, int n, int bs, int nblk, cx<T> *X, const int *pairs_round,
+                   int npairs, const T *gmax2, int inner_sweeps, int *flag) {
+  const T tol = T(4) * sqrt(T(std::max(m, 1))) * Eps<T>::v;
+  const size_t bytes = (size_t)m * 2 * bs * sizeof(cx<T>);
+  cudaFuncSetAttribute(k_bjacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_bjacobi<T><<<npairs, 512, bytes, st>>>(m, n, bs, nblk, X, pairs_round, tol, gmax2, inner_sweeps, flag);
+  count_launch();
+}
+
+template <typename T>
+void colmax2(cudaStream_t st, int m, int n, const cx<T> *X, T *out) {
+  k_colmax2<T><<<1, 1024, 0, st>>>(m, n, X, out);
+  count_launch();
+}
+
+template void bjacobi_round<float>(cudaStream_t, int, int, int, int, cx<float> *, const int *, int, const float *,
+                                   int, int *);
+template void bjacobi_round<double>(cudaStream_t, int, int, int, int, cx<double> *, const int *, int,
+                                    const double *, int, int *);
+template void colmax2<float>(cudaStream_t, int, int, const cx<float> *, float *);
+template void colmax2<double>(cudaStream_t, int, int, const cx<double> *, double *);
 
 template void jacobi_svd<float>(cudaStream_t, int, int, int, const View<float> &, cx<float> *, float *,
                                 cx<float> *, cx<float> *, cx<float> *, int, int *);

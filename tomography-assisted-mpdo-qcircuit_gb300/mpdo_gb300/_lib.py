@@ -37,6 +37,8 @@ SIGNATURES = {
     'mpdo_engine_set_stream': (_I, [_P, _P]),
     'mpdo_engine_set_option': (_I, [_P, C.c_char_p, _D]),
     'mpdo_engine_sync': (_I, [_P]),
+    'mpdo_engine_profile': (_I, [_P, _I]),
+    'mpdo_engine_profile_read': (_I, [_P, _I, C.POINTER(C.c_longlong), _DP, _DP, _DP]),
     'mpdo_engine_launch_count': (_I, [_P, C.POINTER(C.c_uint64)]),
     'mpdo_chain_create': (_I, [_P, _I, _I, _DP, _I, C.POINTER(_P)]),
     'mpdo_chain_destroy': (_I, [_P]),

@@ -78,6 +78,20 @@ class Engine:
                                          m, n, int(keep), _dptr(_cplx(y)), _dptr(lo), _dptr(ro)))
         return lo.view(np.complex128).reshape(m, keep), ro.view(np.complex128).reshape(keep, n)
 
+    KERNEL_CLASSES = ('gemm', 'qr_factor', 'qr_apply', 'jacobi', 'kraus1q', 'mix2q', 'other')
+
+    def profile(self, enable: bool) -> None:
+        check(self._lib.mpdo_engine_profile(self.handle, int(bool(enable))))
+
+    def profile_read(self) -> dict:
+        """{class: dict(launches, ms, flops, bytes)} accumulated since profile(True)."""
+        out = {}
+        for i, name in enumerate(self.KERNEL_CLASSES):
+            n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+            check(self._lib.mpdo_engine_profile_read(self.handle, i, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
+            out[name] = dict(launches=int(n.value), ms=ms.value, flops=fl.value, bytes=by.value)
+        return out
+
     def launch_count(self) -> int:
         c = C.c_uint64()
         check(self._lib.mpdo_engine_launch_count(self.handle, C.byref(c)))
