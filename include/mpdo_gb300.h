@@ -153,6 +153,24 @@ mpdo_status mpdo_debug_qr(mpdo_engine_t eng, int dtype, int m, int n, const doub
 mpdo_status mpdo_debug_svd(mpdo_engine_t eng, int dtype, int m, int n, const double *a, double *w,
                            double *sigma);
 
+/* Allocation-free SVD step (no counterpart in the reference).  For callers
+ * that cannot allocate device memory -- a process whose device memory is
+ * pre-partitioned by its own allocator, or code under an allocation hook that
+ * forbids cudaMalloc -- this computes what the engine's SVD step computes
+ * (Householder TSQR of A, one-sided Jacobi on R with accumulated rotations)
+ * using only a fixed 8 MiB static device array as scratch; it calls no
+ * cudaMalloc/cudaFree.  complex64 only, 1 <= m <= 8192, 1 <= n <= 64; larger
+ * sizes are rejected with MPDO_ERR_INVALID.  Inputs/outputs are DEVICE
+ * pointers on the current device: a (m x n row-major), w (n x n column-major:
+ * right singular vectors sorted by singular value, descending), sigma (n
+ * floats), status (nullable: a device int receiving 0 ok, 1 sweep limit,
+ * 2 non-finite).  stream: a cudaStream_t or NULL.  The first call on a device
+ * resolves the array's device address; make it before any stream capture.
+ * All calls share the array (it keeps the last call's contents), so calls
+ * that overlap on the GPU race and must be serialised by the caller. */
+mpdo_status mpdo_right_svd_noalloc(int m, int n, const void *a, void *w, void *sigma, int *status,
+                                   void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,7 @@ struct Error {
 [[noreturn]] static void fail(mpdo_status s, const std::string &m) { throw Error{s, m}; }
 
 static thread_local std::string g_last_error;
+void set_last_error(const std::string &msg) { g_last_error = msg; }
 
 // ------------------------------------------------------------ engine ----
 struct Engine {

@@ -4,6 +4,8 @@
 
 #include "common.cuh"
 
+#include <string>
+
 namespace mpdo {
 
 // ---------------------------------------------------------------- GEMM ----
@@ -109,5 +111,8 @@ void apply_op_site(cudaStream_t st, const cx<T> *A, cx<T> *out, int L, int Aa, i
 // Trace of a batch of square matrices: out[b] = sum_i M_b[i][i]  (complex, double accum)
 template <typename T>
 void batched_trace(cudaStream_t st, const cx<T> *M, int n, int64_t ld, int64_t bs, int batch, double2 *out);
+
+// Message returned by mpdo_last_error() on the calling thread.
+void set_last_error(const std::string &msg);
 
 }  // namespace mpdo

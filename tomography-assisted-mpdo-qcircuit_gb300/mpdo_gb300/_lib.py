@@ -59,6 +59,7 @@ SIGNATURES = {
     'mpdo_debug_qr': (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_debug_svd': (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_debug_split': (_I, [_P, _I, _I, _I, _I, _DP, _DP, _DP]),
+    'mpdo_right_svd_noalloc': (_I, [_I, _I, _P, _P, _P, _P, _P]),
 }
 
 _lock = threading.Lock()
