@@ -1,0 +1,45 @@
+"""The oracle against the reference's own outputs: the fixtures under
+tests/golden/ were produced by running the reference MPDOSimulator
+(Circuit.py:469-491 evolve, TNNOptimizer.py sweeps, decompositions.py SVD/QR,
+Circuit.py:226-295 cal_dm) on CPU; here the oracle replays the exact gate
+tensors the reference applied and must reproduce its density matrix and the
+leg dimensions of its final state."""
+import numpy as np
+import pytest
+
+import golden_io as G
+from oracle import mpdo_oracle as O
+
+CASES = G.names()
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_oracle_matches_reference(name):
+    info, ops, dm_ref = G.load(name)
+    n = info['qn']
+    st = O.product_state([[1, 0]] * n, connected=False, dtype=G.dtype_of(info))
+    randomized = info['randomized_svd_calls'] > 0
+    O.evolve(st, ops, chi=info['chi'], kappa=info['kappa'], max_err=info['max_truncation_err'],
+             noisy=not info['ideal'], randomized=randomized)
+    rho = O.reduced_dm(st).numpy()
+    for k in range(n):
+        l, _, a, r = st.sites[k].shape
+        assert (l, a, r) == G.expected_dims(info, k), f'site {k} legs'
+    if info['dtype'] == 'complex64':
+        tol = 2e-5
+    elif randomized:
+        # the reference's randomized SVD (decompositions.py:23-48) draws its
+        # test matrix against its own row order; the oracle's emulation draws
+        # the same numbers against the (l, s, a) order, so the two randomized
+        # approximations agree to their own accuracy only (4.8e-6 here; the
+        # exact-SVD oracle is 4.3e-6 away)
+        tol = 1e-5
+    else:
+        tol = 1e-10
+    err = np.abs(rho - dm_ref).max()
+    assert err <= tol * max(1.0, np.abs(dm_ref).max()), f'max |rho - rho_ref| = {err:.3e}'
+
+
+def test_fixtures_present():
+    assert {'noisy_err_c128', 'noisy_err_c64', 'noisy_chi_c128', 'ideal_chi_c128', 'unified_chip_c128',
+            'real_noise_c128'} <= set(CASES)

@@ -40,11 +40,17 @@ class QuantumGate(ABC, nn.Module):
         self.dtype, self.device = dtype, device
 
     def _check_Para_Tensor(self, *parameters):
+        """AbstractGate.py:42-51 casts angles to the circuit's complex dtype, so
+        the trigonometry runs at that precision (an angle given as a float32
+        tensor is widened first).  Angles stay real here, at the matching real
+        precision, which gives the same values and keeps them differentiable."""
+        rdt = torch.float64 if self.dtype == torch.complex128 else torch.float32
+
         def conv(p):
             if isinstance(p, Tensor):
-                return p.to(device=self.device)
+                return p.to(device=self.device, dtype=self.dtype if p.is_complex() else rdt)
             if isinstance(p, (float, int)):
-                return torch.tensor(float(p), dtype=torch.float64, device=self.device)
+                return torch.tensor(float(p), dtype=rdt, device=self.device)
             raise ValueError(f'Invalid type for gate parameter: {type(p)}')
         ps = [conv(p) for p in parameters]
         return ps if len(parameters) > 1 else ps[0]
