@@ -294,8 +294,6 @@ def gpu_arm(args):
     total_ms = allreduce_max(sum(step_ms), ws)
     value = ws * gates_per_step * args.steps / (total_ms / 1e3)
     clocks = clk.summary()
-    last_chain = evs[-1][2]
-    discarded = last_chain.truncate(w.chi, w.kappa, None, True, report=True)
 
     # ---- e2e: public API with host buffers
     dtype = torch.complex64 if args.dtype == 'complex64' else torch.complex128
@@ -311,6 +309,7 @@ def gpu_arm(args):
         if k > 0:
             e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_total = allreduce_max(sum(e2e_ms), ws)
+    dw = [np.asarray(d, dtype=np.float64).ravel() for d in circuit.discarded_weights if d is not None]
     e2e_value = ws * gates_per_step * len(e2e_ms) / (e2e_total / 1e3)
     esz = 8 if args.dtype == 'complex64' else 16
     h2d = w.n * 2 * esz + sum(op[2].size * 16 for op in ops if op[0] != 't')      # vectors + Kraus parameters
@@ -321,6 +320,7 @@ def gpu_arm(args):
     run_chain(ops, w, args.dtype, eng)
     prof = eng.profile_read()
     eng.profile(False)
+    wide = prof.pop('wide_bonds')
     dom = max(prof, key=lambda k: prof[k]['ms'])
     d = prof[dom]
     peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
@@ -358,7 +358,10 @@ def gpu_arm(args):
            'e2e': {'value': e2e_value, 'unit': 'gates/s', 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': d2h,
                    'ms_per_step': e2e_total / len(e2e_ms)},
            'gpu_launches': int(launches), 'clocks': clocks, 'roofline': roof, 'kernel_breakdown_ms': breakdown,
-           'discarded_weight_last_layer_max': float(np.max(discarded)) if discarded is not None else None,
+           'wide_bond_svd': wide,
+           'discarded_weight': {'per_bond_max': max((float(d.max()) for d in dw if d.size), default=None),
+                                'last_truncation_sum': float(dw[-1].sum()) if dw else None,
+                                'truncations': len(dw)},
            'marginal_q0': [float(x) for x in marg.tolist()]}
     print('gpu part: ' + json.dumps(out), file=sys.stderr, flush=True)
     if ws == 1 and not args.no_cpu_baseline:

@@ -70,6 +70,11 @@ mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
  *   "fuse_2q"    1 (default): a 2q gate followed by truncate() is fused into
  *                the QR sweep; 0: always split theta by SVD first (the
  *                reference's exact sequence, including its split cutoff).
+ *   "wide_range" on bonds too wide for one CTA, first try a verified
+ *                randomized range finder (accepted only when the residual
+ *                outside its span is at rounding level, so the triplets are
+ *                those of an exact SVD): 1 always, 0 never (Gram +
+ *                block-Jacobi path only), -1 (default) complex128 only.
  *   "max_sweeps" Jacobi sweep limit (default 60). */
 mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double value);
 /* Wait for all queued work; returns the first deferred device status
@@ -79,7 +84,10 @@ mpdo_status mpdo_engine_sync(mpdo_engine_t eng);
  * every launch is bracketed by CUDA events on the engine stream and its
  * algorithmic flop and byte counts are accumulated.  Classes: 0 GEMM,
  * 1 Householder QR factor, 2 QR explicit-Q apply, 3 one-sided Jacobi,
- * 4 Kraus 1q apply, 5 two-site gate mix, 6 other.  Enabling resets the sums. */
+ * 4 Kraus 1q apply, 5 two-site gate mix, 6 other.  Class 7 returns counters
+ * instead: launches = wide bonds solved by the range finder, flops = wide
+ * bonds solved by the exact block Jacobi, bytes = the largest accepted relative
+ * residual |Y - Q Q^H Y|_F / |Y|_F.  Enabling resets the sums. */
 mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable);
 mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *launches, double *ms,
                                      double *flops, double *bytes);

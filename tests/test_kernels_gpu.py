@@ -99,3 +99,52 @@ def test_split_wide_rank_deficient(eng, m, n, keep, rank, dtype, tol):
     k = min(keep, len(s))
     best = (u[:, :k] * s[:k]) @ vh[:k]
     np.testing.assert_allclose(L @ R, best, atol=tol * s[0] * 10)
+
+
+def _decaying(m, n, seed, decades_per_sv):
+    rng = np.random.default_rng(seed)
+    u, _ = np.linalg.qr(rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m)))
+    v, _ = np.linalg.qr(rng.normal(size=(n, m)) + 1j * rng.normal(size=(n, m)))
+    s = 10.0 ** (-np.arange(m) * decades_per_sv)
+    return (u * s) @ v.conj().T
+
+
+@pytest.mark.parametrize('decay,expect_range', [(0.25, True), (0.01, False)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-4)])
+def test_split_wide_range_finder(eng, decay, expect_range, dtype, tol):
+    # wide bonds first try the randomized range finder; it is accepted only when
+    # the residual outside its span is at rounding level (fast-decaying
+    # spectrum), otherwise the exact block-Jacobi path runs.  Both must give the
+    # best rank-keep approximation.
+    m, n, keep = 256, 2048, 64
+    y = _decaying(m, n, 21, decay)
+    eng.profile(True)
+    eng.set_option('wide_range', 1)
+    try:
+        L, R = eng.debug_split(y, keep, dtype)
+    finally:
+        eng.set_option('wide_range', -1)
+    wide = eng.profile_read()['wide_bonds']
+    eng.profile(False)
+    assert (wide['range_finder'], wide['exact']) == ((1, 0) if expect_range else (0, 1))
+    u, s, vh = np.linalg.svd(y, full_matrices=False)
+    best = (u[:, :keep] * s[:keep]) @ vh[:keep]
+    np.testing.assert_allclose(L @ R, best, atol=tol * s[0] * 10)
+    g = L.conj().T @ L
+    np.testing.assert_allclose(np.diag(g).real, s[:keep], atol=tol * s[0])
+    assert np.abs(g - np.diag(np.diag(g))).max() <= tol * s[0]
+
+
+@pytest.mark.parametrize('dtype', ['complex128', 'complex64'])
+def test_split_wide_range_matches_exact(eng, dtype):
+    # the same split through both wide paths (option wide_range on / off)
+    y = _decaying(256, 4096, 5, 0.1)
+    try:
+        eng.set_option('wide_range', 1)
+        L1, R1 = eng.debug_split(y, 64, dtype)
+        eng.set_option('wide_range', 0)
+        L0, R0 = eng.debug_split(y, 64, dtype)
+    finally:
+        eng.set_option('wide_range', -1)
+    tol = 1e-11 if dtype == 'complex128' else 2e-5
+    np.testing.assert_allclose(L1 @ R1, L0 @ R0, atol=tol * np.abs(L0 @ R0).max() * 10)

@@ -53,6 +53,9 @@ struct Engine {
   int status_cap = 8192;
   int status_used = 0;
   bool fuse_2q = true;
+  int wide_range = -1;              // verified range finder on wide bonds: 1 on, 0 off, -1 complex128 only
+  long long wide_range_hits = 0, wide_exact_calls = 0;
+  double wide_resid_max = 0;        // largest accepted |Y - Q Q^H Y|_F / |Y|_F
   int max_sweeps = 60;
   int first_status = 0;
   // per-kernel-class profiling (CUDA events around each launch)
@@ -339,8 +342,8 @@ static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
 // Z = U^H Y), which restores the accuracy of the small singular values.
 // U: Mr x kr column-major; s: Mr values (kr refined, the rest from the Gram).
 template <typename T>
-static void left_svd_wide(Engine &e, const cx<T> *Y, int Mr, int Nc, int want, DBuf<cx<T>> &U, DBuf<T> &s,
-                          int &kr) {
+static void left_svd_wide_exact(Engine &e, const cx<T> *Y, int Mr, int Nc, int want, DBuf<cx<T>> &U, DBuf<T> &s,
+                                int &kr) {
   DBuf<cx<T>> G(e, (size_t)Mr * Mr), X(e, (size_t)Mr * Mr);
   gemm<T>(e, Mr, Mr, Nc, RM<T>(Y, Nc), CM<T>(Y, Nc, 1), G.p, Mr);
   {  // X (column-major) = G^T = conj(G) for a Hermitian G stored row-major
@@ -384,6 +387,86 @@ static void left_svd_wide(Engine &e, const cx<T> *Y, int Mr, int Nc, int want, D
     sqrt_inplace<T>(e.stream, lam.p, Mr);
     MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p + kr, lam.p + kr, (Mr - kr) * sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
   }
+}
+
+// Verified randomized range finder for a wide bond: Q = orth(Y Omega) with
+// p = want + 32 columns (optionally one power step Q <- orth(Y Y^H Q)), then the
+// exact SVD of B = Q^H Y (QR + one-sided Jacobi).  The result is accepted only
+// if the residual |Y - Q B|_F is below working precision relative to |Y|_F:
+// then span(Q) holds the whole numerical range of Y and the singular triplets
+// equal those of an exact SVD to rounding.  Returns false (caller falls back
+// to the exact block-Jacobi path) otherwise.
+template <typename T>
+static bool left_svd_wide_range(Engine &e, const cx<T> *Y, int Mr, int Nc, int want, DBuf<cx<T>> &U, DBuf<T> &s,
+                                int &kr) {
+  const int p = std::min(Mr, std::min(Nc, want + 32));
+  if (p >= Mr) return false;
+  const T eps = sizeof(T) == 4 ? T(1.1920929e-7) : T(2.220446049250313e-16);
+  // rounding level of the residual itself: |fl(Y - Q (Q^H Y))|_F ~ eps sqrt(p) |Y|_F
+  const double tol = 8.0 * eps * std::sqrt((double)p);
+  DBuf<double> nrm(e, 2);
+  sumsq<T>(e.stream, Y, (size_t)Mr * Nc, nrm.p);
+  DBuf<cx<T>> Z(e, (size_t)Mr * p), Q(e, (size_t)Mr * p), Rq(e, (size_t)p * p), B(e, (size_t)p * Nc),
+      E(e, (size_t)Mr * Nc);
+  {
+    DBuf<cx<T>> Om(e, (size_t)Nc * p);
+    gaussian<T>(e.stream, Om.p, (size_t)Nc * p, 0x5eed5eedull + (uint64_t)Nc * 131 + p);
+    gemm<T>(e, Mr, p, Nc, RM<T>(Y, Nc), RM<T>(Om.p, p), Z.p, p);
+  }
+  bool ok = false;
+  for (int it = 0; it < 2 && !ok; ++it) {
+    qr<T>(e, Mr, p, RM<T>(Z.p, p), Q.p, Rq.p);
+    gemm<T>(e, p, Nc, Mr, CM<T>(Q.p, p, 1), RM<T>(Y, Nc), B.p, Nc);          // B = Q^H Y
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(E.p, Y, (size_t)Mr * Nc * sizeof(cx<T>), cudaMemcpyDeviceToDevice, e.stream));
+    prof(e, K_GEMM, 8.0 * Mr * Nc * p, (double)sizeof(cx<T>) * ((double)Mr * p + (double)p * Nc + 2.0 * Mr * Nc), [&] {
+      cgemm<T>(e.stream, Mr, Nc, p, 1, cmk<T>(T(-1), T(0)), RM<T>(Q.p, p), RM<T>(B.p, Nc), cmk<T>(T(1), T(0)), E.p,
+               Nc, 1, 0);                                                  // E = Y - Q B
+    });
+    sumsq<T>(e.stream, E.p, (size_t)Mr * Nc, nrm.p + 1);
+    double h[2];
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(h, nrm.p, sizeof(h), cudaMemcpyDeviceToHost, e.stream));
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+    const double ratio = h[0] > 0.0 ? std::sqrt(h[1] / h[0]) : 0.0;
+    ok = ratio <= tol;
+    if (ok) {
+      e.wide_resid_max = std::max(e.wide_resid_max, ratio);
+      break;
+    }
+    // one power step squares the captured/missed ratio; beyond reach of one
+    // step (a heavy tail past p) go straight to the exact path
+    if (it == 1 || ratio > 1e3 * tol) break;
+    gemm<T>(e, Mr, p, Nc, RM<T>(Y, Nc), CM<T>(B.p, Nc, 1), Z.p, p);      // Z = Y B^H = Y Y^H Q
+  }
+  if (!ok) return false;
+  E.reset();
+  DBuf<cx<T>> Wb;
+  DBuf<T> sb;
+  right_svd<T>(e, Nc, p, CM<T>(B.p, Nc, 1), Wb, sb);             // left singular vectors of B
+  DBuf<cx<T>> Urm(e, (size_t)Mr * p);
+  gemm<T>(e, Mr, p, p, RM<T>(Q.p, p), CM<T>(Wb.p, p), Urm.p, p);
+  U = DBuf<cx<T>>(e, (size_t)Mr * p);
+  {
+    const int64_t d[4] = {1, 1, p, Mr};
+    const int64_t st[4] = {0, 0, 1, p};
+    copy4d<T>(e.stream, U.p, Urm.p, d, st, 0);
+  }
+  s = DBuf<T>(e, Mr);
+  MPDO_CUDA_CHECK(cudaMemsetAsync(s.p, 0, Mr * sizeof(T), e.stream));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p, sb.p, p * sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
+  kr = p;
+  return true;
+}
+
+template <typename T>
+static void left_svd_wide(Engine &e, const cx<T> *Y, int Mr, int Nc, int want, DBuf<cx<T>> &U, DBuf<T> &s,
+                          int &kr) {
+  const bool try_range = e.wide_range > 0 || (e.wide_range < 0 && sizeof(T) == 8);
+  if (try_range && left_svd_wide_range<T>(e, Y, Mr, Nc, want, U, s, kr)) {
+    e.wide_range_hits++;
+    return;
+  }
+  e.wide_exact_calls++;
+  left_svd_wide_exact<T>(e, Y, Mr, Nc, want, U, s, kr);
 }
 
 // --------------------------------------------------------- SVD split ----
@@ -954,7 +1037,7 @@ static void debug_split(Engine &e, int Mr, int Nc, int keep, const double *y, do
   DBuf<cx<T>> Y(e, hy.size()), Lf, Rf;
   MPDO_CUDA_CHECK(cudaMemcpyAsync(Y.p, hy.data(), hy.size() * sizeof(cx<T>), cudaMemcpyHostToDevice, e.stream));
   int kept = 0;
-  svd_split<T>(e, Y.p, Mr, Nc, [&](const T *, int) { return keep; }, Lf, Rf, kept, nullptr);
+  svd_split<T>(e, Y.p, Mr, Nc, [&](const T *, int) { return keep; }, Lf, Rf, kept, nullptr, keep);
   std::vector<cx<T>> hl((size_t)Mr * keep), hr((size_t)keep * Nc);
   MPDO_CUDA_CHECK(cudaMemcpyAsync(hl.data(), Lf.p, hl.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
   MPDO_CUDA_CHECK(cudaMemcpyAsync(hr.data(), Rf.p, hr.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, e.stream));
@@ -1054,6 +1137,7 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
     const std::string k(name);
     Engine &e = eng->e;
     if (k == "fuse_2q") e.fuse_2q = value != 0;
+    else if (k == "wide_range") e.wide_range = value > 0 ? 1 : (value < 0 ? -1 : 0);
     else if (k == "max_sweeps") { need(value >= 1 && value <= 1000, "max_sweeps out of range"); e.max_sweeps = (int)value; }
     else fail(MPDO_ERR_INVALID, "unknown option: " + k);
   });
@@ -1065,6 +1149,8 @@ mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable) {
     Engine &e = eng->e;
     prof_flush(e);
     for (int c = 0; c < 8; ++c) { e.acc_ms[c] = e.acc_flops[c] = e.acc_bytes[c] = 0; e.acc_n[c] = 0; }
+    e.wide_range_hits = e.wide_exact_calls = 0;
+    e.wide_resid_max = 0;
     e.profiling = enable != 0;
   });
 }
@@ -1076,6 +1162,13 @@ mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *l
     need(kclass >= 0 && kclass < 8, "kernel class out of range");
     Engine &e = eng->e;
     prof_flush(e);
+    if (kclass == 7) {   // wide-bond SVD path counters: range finder accepted / exact block Jacobi
+      *launches = e.wide_range_hits;
+      *ms = 0;
+      *flops = (double)e.wide_exact_calls;
+      *bytes = e.wide_resid_max;
+      return;
+    }
     *launches = e.acc_n[kclass];
     *ms = e.acc_ms[kclass];
     *flops = e.acc_flops[kclass];

@@ -112,6 +112,13 @@ void apply_op_site(cudaStream_t st, const cx<T> *A, cx<T> *out, int L, int Aa, i
 template <typename T>
 void batched_trace(cudaStream_t st, const cx<T> *M, int n, int64_t ld, int64_t bs, int batch, double2 *out);
 
+// Deterministic complex Gaussian test matrix (re, im ~ N(0, 1/2)).
+template <typename T>
+void gaussian(cudaStream_t st, cx<T> *out, size_t n, uint64_t seed);
+// *out = sum |x_i|^2 (double accumulation; *out is cleared first)
+template <typename T>
+void sumsq(cudaStream_t st, const cx<T> *x, size_t n, double *out);
+
 // Message returned by mpdo_last_error() on the calling thread.
 void set_last_error(const std::string &msg);
 

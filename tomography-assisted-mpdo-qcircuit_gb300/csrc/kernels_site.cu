@@ -168,6 +168,39 @@ __global__ void k_apply_op(const cx<T> *A, cx<T> *out, int L, int Aa, int R, cx<
   }
 }
 
+// Deterministic Gaussian test matrix: splitmix64 counter hash -> two uniforms
+// -> Box-Muller; real and imaginary parts N(0, 1/2).
+__device__ __forceinline__ uint64_t smix(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+template <typename T>
+__global__ void k_gauss(cx<T> *out, size_t n, uint64_t seed) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const uint64_t h1 = smix(seed ^ (2 * t)), h2 = smix(seed ^ (2 * t + 1));
+    const double u1 = ((h1 >> 11) + 1.0) * (1.0 / 9007199254740993.0);   // (0, 1]
+    const double u2 = (h2 >> 11) * (1.0 / 9007199254740992.0);
+    const double r = sqrt(-log(u1)), th = 6.283185307179586 * u2;
+    out[t] = cmk<T>((T)(r * cos(th)), (T)(r * sin(th)));
+  }
+}
+template <typename T>
+__global__ void k_sumsq(const cx<T> *x, size_t n, double *out) {
+  __shared__ double red[256];
+  double a = 0;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    a += (double)x[t].x * x[t].x + (double)x[t].y * x[t].y;
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(out, red[0]);
+}
+
 template <typename T>
 __global__ void k_trace(const cx<T> *M, int n, int64_t ld, int64_t bs, int batch, double2 *out) {
   for (int b = blockIdx.x; b < batch; b += gridDim.x) {
@@ -269,6 +302,19 @@ void batched_trace(cudaStream_t st, const cx<T> *M, int n, int64_t ld, int64_t b
   count_launch();
 }
 
+template <typename T>
+void gaussian(cudaStream_t st, cx<T> *out, size_t n, uint64_t seed) {
+  k_gauss<T><<<nblocks((int64_t)n), 256, 0, st>>>(out, n, seed);
+  count_launch();
+}
+
+template <typename T>
+void sumsq(cudaStream_t st, const cx<T> *x, size_t n, double *out) {
+  cudaMemsetAsync(out, 0, sizeof(double), st);
+  k_sumsq<T><<<std::min<int64_t>(nblocks((int64_t)n), 1024), 256, 0, st>>>(x, n, out);
+  count_launch();
+}
+
 #define INST(T)                                                                                             \
   template void kraus1q<T>(cudaStream_t, const cx<T> *, cx<T> *, int, int, int, const double *, int);      \
   template void mix2q<T>(cudaStream_t, const cx<T> *, cx<T> *, int, int, int, const double *, int);        \
@@ -281,7 +327,9 @@ void batched_trace(cudaStream_t st, const cx<T> *M, int n, int64_t ld, int64_t b
   template void sigma_weights<T>(cudaStream_t, const T *, int, int, double *);                             \
   template void sqrt_inplace<T>(cudaStream_t, T *, int);                                                   \
   template void apply_op_site<T>(cudaStream_t, const cx<T> *, cx<T> *, int, int, int, const double *);      \
-  template void batched_trace<T>(cudaStream_t, const cx<T> *, int, int64_t, int64_t, int, double2 *);
+  template void batched_trace<T>(cudaStream_t, const cx<T> *, int, int64_t, int64_t, int, double2 *);       \
+  template void gaussian<T>(cudaStream_t, cx<T> *, size_t, uint64_t);                                     \
+  template void sumsq<T>(cudaStream_t, const cx<T> *, size_t, double *);
 INST(float)
 INST(double)
 #undef INST

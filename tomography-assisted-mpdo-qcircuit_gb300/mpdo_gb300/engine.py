@@ -90,6 +90,9 @@ class Engine:
             n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
             check(self._lib.mpdo_engine_profile_read(self.handle, i, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
             out[name] = dict(launches=int(n.value), ms=ms.value, flops=fl.value, bytes=by.value)
+        n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+        check(self._lib.mpdo_engine_profile_read(self.handle, 7, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
+        out['wide_bonds'] = dict(range_finder=int(n.value), exact=int(fl.value), max_residual=by.value)
         return out
 
     def launch_count(self) -> int:
