@@ -1,28 +1,38 @@
 #!/usr/bin/env python
 """Benchmark of the MPDO noisy-circuit hot path (gates/s).
 
-Workload (default): n=32 qubits, depth 20 (U3 on every qubit, then CZ/CNOT
-brickwork, seed 0), 1q depolarising 1e-3 + amplitude damping 1e-3 after every
-1q gate, 2q depolarising 1e-2 after every 2q gate, a truncate() after every
-sublayer, chi=64, kappa=4, complex64.  One step = one full evolution of that
-circuit (960 gates, 40 truncate layers).
+Circuit (the n=32, chi=64, kappa=4 workload): 32 qubits, depth 20 (U3 on every
+qubit, then CZ/CNOT brickwork), 1q depolarising 1e-3 + amplitude damping 1e-3
+after every 1q gate, 2q depolarising 1e-2 after every 2q gate, a truncate()
+after every sublayer, complex64; 950 gates and 40 truncate layers.
 
-value: gates/s with the circuit's Kraus tensors prepared on the host and the
-       state created on the device, CUDA events on the engine's stream around
-       the K timed steps (L2 flushed between steps).
-e2e:   the same through the drop-in API (TensorCircuit.evolve from a host
-       product state, then a device->host read of a single-qubit marginal).
-roofline: per-kernel-class CUDA-event timing of one extra step; the dominant
-       class's algorithmic flops (or bytes) / its time against the measured peak.
+One step = one batch of --batch independent circuits of that shape (seeds
+0..B-1) through the batched engine (--workers worker engines, each with its
+own stream and memory pool).
+value: gates/s over the K timed steps, CUDA events on an idle stream around
+       the synchronous batch call (Kraus tensors are host data by design: they
+       travel as kernel parameters), L2 flushed between steps.
+e2e:   the same circuits through the public API (MPDOSimulator.evolve_batch on
+       TensorCircuit objects built per step, host product states in, <Z_i>,
+       <Z_i Z_i+1> and per-bond discarded weights out).
+plain: one circuit through one engine (CUDA events on its stream) and through
+       TensorCircuit.evolve, with its own roofline and kernel breakdown.
+roofline: per-kernel-class CUDA-event timing of one extra batch; the dominant
+       class's algorithmic flops (or bytes) / its summed launch time against
+       the measured peak.
 cpu_baseline / --impl reference: the CPU oracle (restatement of the reference
-       path, torch CPU, exact SVD) on a steady-state layer of the same circuit.
+       path, torch CPU, exact SVD) on a steady-state layer of the seed-0
+       circuit (the reference evolves circuits one after another).
 
-Multi-GPU (torchrun, N > 1): independent replicas of the circuit, one per GPU
-(the path does not shard within a circuit); value = total gates / max time.
+Multi-GPU (torchrun, N > 1): independent replicas, each rank its own batch of
+seeds; value = total gates / max time over ranks.
 """
 import argparse
 import json
 import os
+
+# one hardware work queue per batch worker stream (must precede CUDA init)
+os.environ.setdefault('CUDA_DEVICE_MAX_CONNECTIONS', '32')
 import statistics
 import subprocess
 import sys
@@ -52,6 +62,10 @@ def parse():
     ap.add_argument('--dtype', default='complex64')
     ap.add_argument('--cpu-budget', type=float, default=20.0, help='seconds of CPU work for the baseline sample')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--batch', type=int, default=16, help='independent circuits per step (seeds)')
+    ap.add_argument('--workers', type=int, default=16, help='worker engines of the batch runner')
+    ap.add_argument('--plain-steps', type=int, default=1, help='timed single-circuit runs (reported as plain)')
+    ap.add_argument('--plain-warmup', type=int, default=1)
     return ap.parse_args()
 
 
@@ -84,48 +98,38 @@ def allreduce_max(x, ws):
 
 
 # --------------------------------------------------------------- workload --
-def workload(args):
+def workload(args, seed=0):
     from mpdo_gb300.workloads import config1
-    return config1(n=args.n, depth=args.depth, chi=args.chi, kappa=args.kappa)
+    return config1(n=args.n, depth=args.depth, chi=args.chi, kappa=args.kappa, seed=seed)
 
 
 def host_ops(w, dtype):
-    """Kraus tensors of every gate, built by the drop-in API's own builders."""
-    import numpy as np
+    """The circuit as the drop-in API builds it and the engine operations its
+    evolve() performs (Kraus tensors by the API's own builders)."""
     import torch
     from mpdo_gb300.workloads import build_circuit
     c = build_circuit(w, dtype=torch.complex64 if dtype == 'complex64' else torch.complex128, device='cuda:0')
-    ops = []
-    for i, layer in enumerate(c.layers):
-        name = layer.name.lower()
-        if 'truncate' in name:
-            ops.append(('t',))
-            continue
-        oqs = c._oqs_list[i]
-        if layer.single:
-            ops.append(('1', oqs[0], np.ascontiguousarray(c._noisy_1q(layer))))
-        else:
-            t = c._noisy_2q(layer)
-            if t.ndim == 4:
-                t = t[..., None]
-            a, b = oqs
-            if a > b:
-                t = np.transpose(t, (1, 0, 3, 2, 4))
-            ops.append(('2', min(a, b), np.ascontiguousarray(t)))
-    return c, ops
+    return c, c._engine_ops()
 
 
 def run_chain(ops, w, dtype, eng):
     from mpdo_gb300 import Chain
     ch = Chain([[1, 0]] * w.n, dtype=dtype, connected=True, engine=eng)
     for op in ops:
-        if op[0] == '1':
+        if op[0] == '1q':
             ch.apply_1q(op[1], op[2])
-        elif op[0] == '2':
+        elif op[0] == '2q':
             ch.apply_2q(op[1], op[2], 2.718281828459045e-8)
-        else:
+        elif op[0] == 'truncate':
             ch.truncate(w.chi, w.kappa, None, True)
+        else:
+            ch.kappa_truncate(w.kappa, None)
     return ch
+
+
+def program(w, ops, dtype):
+    return dict(n=w.n, dtype=dtype, vectors=[[1, 0]] * w.n, connected=True, chi=w.chi, kappa=w.kappa,
+                max_err=None, noisy=True, ops=ops, z=True, zz=True, discarded=True)
 
 
 # ----------------------------------------------------------------- clocks --
@@ -241,90 +245,20 @@ def reference_arm(args):
     out = {'metric': METRIC, 'value': val, 'unit': 'gates/s', 'n_gpus': args.gpus, 'steps': args.steps,
            'warmup': args.warmup, 'ms_per_step': 1e3 * gates / val, 'higher_is_better': True, 'scaling': 'weak',
            'vs_baseline': None, 'dtype': 'c64', 'data': 'synthetic', 'impl': 'reference',
-           'config': {'workload': w.name, 'n': w.n, 'depth': w.depth, 'chi': w.chi, 'kappa': w.kappa,
-                      'step': 'one steady-state layer (sample)'},
+           'config': {'workload': f'{max(1, args.batch)} independent circuits of {w.name}, seeds 0..'
+                                  f'{max(1, args.batch) - 1}', 'n': w.n, 'depth': w.depth, 'chi': w.chi,
+                      'kappa': w.kappa, 'circuits_per_step': max(1, args.batch),
+                      'step': 'circuits run one after another; each step times a sample: one steady-state '
+                              'layer of the seed-0 circuit'},
            'cpu_baseline': {'value': val, 'unit': 'gates/s', 'cores': th, 'kind': 'port', 'sample': sample},
            'e2e': {'value': val, 'unit': 'gates/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(out), flush=True)
 
 
 # --------------------------------------------------------------- GPU arm --
-def gpu_arm(args):
-    import numpy as np
-    import torch
-    rank, ws, local = dist_init(args)
-    torch.cuda.set_device(local)
-    import mpdo_gb300
-    mpdo_gb300.build()
-    from mpdo_gb300 import Engine
-    import MPDOSimulator as S
-    eng = Engine.get(local)
-    # one explicit stream shared by torch (events, L2 flush) and the engine
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    eng.set_stream(stream.cuda_stream)
-    w = workload(args)
-    circuit, ops = host_ops(w, args.dtype)
-    gates_per_step = w.gates
-
-    # warm-up
-    for _ in range(args.warmup):
-        run_chain(ops, w, args.dtype, eng)
-    torch.cuda.synchronize()
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device='cuda')   # 256 MB > L2
-
-    # ---- value: device-resident inputs, CUDA events on the engine stream
-    barrier(ws)
-    torch.cuda.synchronize()
-    launches0 = eng.launch_count()
-    evs = []
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            ch = run_chain(ops, w, args.dtype, eng)
-            b.record(stream)
-            evs.append((a, b, ch))
-        torch.cuda.synchronize()
-    barrier(ws)
-    launches = eng.launch_count() - launches0
-    eng.sync()
-    step_ms = [a.elapsed_time(b) for a, b, _ in evs]
-    total_ms = allreduce_max(sum(step_ms), ws)
-    value = ws * gates_per_step * args.steps / (total_ms / 1e3)
-    clocks = clk.summary()
-
-    # ---- e2e: public API with host buffers
-    dtype = torch.complex64 if args.dtype == 'complex64' else torch.complex128
-    e2e_ms = []
-    for k in range(args.steps + 1):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        state = S.Tools.create_ket0Series(w.n, dtype=dtype, connected=True)
-        circuit.evolve(state)
-        marg = circuit.probabilities([0])
-        torch.cuda.synchronize()
-        if k > 0:
-            e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_total = allreduce_max(sum(e2e_ms), ws)
-    dw = [np.asarray(d, dtype=np.float64).ravel() for d in circuit.discarded_weights if d is not None]
-    e2e_value = ws * gates_per_step * len(e2e_ms) / (e2e_total / 1e3)
-    esz = 8 if args.dtype == 'complex64' else 16
-    h2d = w.n * 2 * esz + sum(op[2].size * 16 for op in ops if op[0] != 't')      # vectors + Kraus parameters
-    d2h = 8 * 2 + 8 * (w.n - 1) * w.gate_layers                                   # marginal + discarded weights
-
-    # ---- roofline: one profiled step
-    eng.profile(True)
-    run_chain(ops, w, args.dtype, eng)
-    prof = eng.profile_read()
-    eng.profile(False)
-    wide = prof.pop('wide_bonds')
+def _roofline(prof, peaks):
     dom = max(prof, key=lambda k: prof[k]['ms'])
     d = prof[dom]
-    peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
-        os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
     if dom in ('kraus1q', 'mix2q', 'other'):
         achieved = d['bytes'] / (d['ms'] / 1e3) / 1e9
         peak = peaks.get('hbm_gbs', 6800.0)
@@ -337,38 +271,168 @@ def gpu_arm(args):
                 'frac_of_fp32_simt_nominal': achieved / FP32_SIMT_NOMINAL_TFLOPS}
         per_launch_alg = d['flops'] / max(1, d['launches'])
     roof.update({'kernel': dom, 'peak_source': 'measured (MEASURED_PEAKS.json)' if peaks else 'fallback',
-                 'launches_per_step': d['launches'], 'ms_per_step': d['ms'], 'share_of_step': d['ms'] / (sum(
-                     v['ms'] for v in prof.values()) or 1), 'algorithmic_per_launch': per_launch_alg,
-                 'traffic': None})
+                 'launches': d['launches'], 'kernel_ms': d['ms'],
+                 'share_of_kernel_time': d['ms'] / (sum(v['ms'] for v in prof.values()) or 1),
+                 'algorithmic_per_launch': per_launch_alg, 'traffic': None})
     tfile = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tfile):
         tr = json.load(open(tfile)).get(dom)
         if tr:
             roof['traffic'] = tr.get('bytes_per_launch')
-    breakdown = {k: {'launches': v['launches'], 'ms': round(v['ms'], 3)} for k, v in prof.items() if v['launches']}
+    return roof
 
+
+def _sum_profiles(profs):
+    out = {}
+    for p in profs:
+        for k, v in p.items():
+            if k == 'wide_bonds':
+                continue
+            o = out.setdefault(k, dict(launches=0, ms=0.0, flops=0.0, bytes=0.0))
+            for f in o:
+                o[f] += v[f]
+    return out
+
+
+def gpu_arm(args):
+    import numpy as np
+    import torch
+    rank, ws, local = dist_init(args)
+    torch.cuda.set_device(local)
+    import mpdo_gb300
+    mpdo_gb300.build()
+    from mpdo_gb300 import Batch, Engine
+    import MPDOSimulator as S
+    from mpdo_gb300.workloads import build_circuit
+    peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))) if os.path.exists(
+        os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
+    cdt = torch.complex64 if args.dtype == 'complex64' else torch.complex128
+    B = max(1, args.batch)
+    seeds = [rank * B + k for k in range(B)]
+    works = [workload(args, seed=s) for s in seeds]
+    w = works[0]
+    gates_per_circuit = w.gates
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device='cuda')   # 256 MB > L2
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    # ---- plain path: one circuit through one engine (device-resident inputs)
+    eng = Engine.get(local)
+    eng.set_stream(stream.cuda_stream)
+    circuit, ops = host_ops(w, args.dtype)
+    for _ in range(args.plain_warmup):
+        run_chain(ops, w, args.dtype, eng)
+    torch.cuda.synchronize()
+    plain_ms = []
+    for _ in range(args.plain_steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run_chain(ops, w, args.dtype, eng)
+        b.record(stream)
+        b.synchronize()
+        plain_ms.append(a.elapsed_time(b))
+    eng.sync()
+    eng.profile(True)
+    run_chain(ops, w, args.dtype, eng)
+    plain_prof = eng.profile_read()
+    eng.profile(False)
+    plain_wide = plain_prof.pop('wide_bonds')
+    t0 = time.perf_counter()
+    circuit.evolve(S.Tools.create_ket0Series(w.n, dtype=cdt, connected=True))
+    marg = circuit.probabilities([0])
+    torch.cuda.synchronize()
+    plain_e2e_ms = 1e3 * (time.perf_counter() - t0)
+    dw = [np.asarray(d, dtype=np.float64).ravel() for d in circuit.discarded_weights if d is not None]
+    plain = {'value': gates_per_circuit / (statistics.mean(plain_ms) / 1e3), 'unit': 'gates/s',
+             'ms_per_circuit': statistics.mean(plain_ms), 'steps': args.plain_steps, 'warmup': args.plain_warmup,
+             'e2e_value': gates_per_circuit / (plain_e2e_ms / 1e3), 'e2e_ms': plain_e2e_ms,
+             'roofline': _roofline(plain_prof, peaks),
+             'kernel_breakdown_ms': {k: {'launches': v['launches'], 'ms': round(v['ms'], 3)}
+                                     for k, v in plain_prof.items() if v['launches']},
+             'wide_bond_svd': plain_wide,
+             'discarded_weight': {'per_bond_max': max((float(d.max()) for d in dw if d.size), default=None),
+                                  'last_truncation_sum': float(dw[-1].sum()) if dw else None,
+                                  'truncations': len(dw)},
+             'marginal_q0': [float(x) for x in marg.tolist()]}
+    eng.set_stream(None)
+
+    # ---- batched: B independent circuits (seeds) on W worker engines
+    batch = Batch.get(local, args.workers)
+    progs = [program(wk, host_ops(wk, args.dtype)[1], args.dtype) for wk in works]
+    for _ in range(args.warmup):
+        batch.run(progs)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches0 = eng.launch_count()
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            stream.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            res = batch.run(progs)          # returns once every worker engine has synchronised
+            b.record(stream)
+            b.synchronize()
+            step_ms.append(a.elapsed_time(b))
+    barrier(ws)
+    launches = eng.launch_count() - launches0
+    clocks = clk.summary()
+    total_ms = allreduce_max(sum(step_ms), ws)
+    value = ws * B * gates_per_circuit * args.steps / (total_ms / 1e3)
+    for e in batch.engines:
+        e.profile(True)
+    batch.run(progs)
+    bprofs = [e.profile_read() for e in batch.engines]
+    for e in batch.engines:
+        e.profile(False)
+    bprof = _sum_profiles(bprofs)
+    wide = {'range_finder': sum(p['wide_bonds']['range_finder'] for p in bprofs),
+            'exact': sum(p['wide_bonds']['exact'] for p in bprofs)}
+
+    # ---- batched e2e: the public API with host inputs and host results
+    e2e_ms = []
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cs = [build_circuit(wk, dtype=cdt, device=f'cuda:{local}') for wk in works]
+        out = S.evolve_batch(cs, [S.Tools.create_ket0Series(wk.n, dtype=cdt, connected=True) for wk in works],
+                             workers=args.workers)
+        zs = [np.asarray(r['z']) for r in out]
+        torch.cuda.synchronize()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_total = allreduce_max(sum(e2e_ms), ws)
+    e2e_value = ws * B * gates_per_circuit * len(e2e_ms) / (e2e_total / 1e3)
+    h2d = sum(sum(op[2].size * 16 for op in p['ops'] if len(op) > 2) + w.n * 32 for p in progs)
+    d2h = B * 8 * (w.n + (w.n - 1) + (w.n - 1) * w.gate_layers)
     if rank != 0:
         return
+    z0 = [float(x) for x in zs[0][:4]]
     out = {'metric': METRIC, 'value': value, 'unit': 'gates/s', 'n_gpus': ws, 'steps': args.steps,
            'warmup': args.warmup, 'ms_per_step': total_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak',
            'vs_baseline': None, 'dtype': 'c64' if args.dtype == 'complex64' else 'c128', 'data': 'synthetic',
-           'config': {'workload': w.name, 'n': w.n, 'depth': w.depth, 'chi': w.chi, 'kappa': w.kappa,
-                      'gates_per_step': gates_per_step, 'gate_layers_per_step': w.gate_layers,
-                      'parallelism': f'replicas{ws}', 'l2': 'flushed between steps (256 MB write)'},
+           'config': {'workload': f'{B} independent circuits of {w.name}, seeds {seeds[0]}..{seeds[-1]}',
+                      'n': w.n, 'depth': w.depth, 'chi': w.chi, 'kappa': w.kappa, 'circuits_per_step': B,
+                      'workers': batch.workers, 'gates_per_circuit': gates_per_circuit,
+                      'gate_layers_per_circuit': w.gate_layers, 'parallelism': f'replicas{ws}',
+                      'l2': 'flushed between steps (256 MB write); the per-circuit state is ~8 MB',
+                      'timing': 'CUDA events on an idle stream around the synchronous batch call'},
            'e2e': {'value': e2e_value, 'unit': 'gates/s', 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': d2h,
-                   'ms_per_step': e2e_total / len(e2e_ms)},
-           'gpu_launches': int(launches), 'clocks': clocks, 'roofline': roof, 'kernel_breakdown_ms': breakdown,
-           'wide_bond_svd': wide,
-           'discarded_weight': {'per_bond_max': max((float(d.max()) for d in dw if d.size), default=None),
-                                'last_truncation_sum': float(dw[-1].sum()) if dw else None,
-                                'truncations': len(dw)},
-           'marginal_q0': [float(x) for x in marg.tolist()]}
+                   'ms_per_step': e2e_total / len(e2e_ms),
+                   'path': 'MPDOSimulator.evolve_batch on TensorCircuit objects built per step'},
+           'gpu_launches': int(launches), 'clocks': clocks, 'roofline': _roofline(bprof, peaks),
+           'kernel_breakdown_ms': {k: {'launches': v['launches'], 'ms': round(v['ms'], 3)}
+                                   for k, v in bprof.items() if v['launches']},
+           'wide_bond_svd': wide, 'z_first_circuit': z0,
+           'plain': plain, 'batched_over_plain': value / plain['value']}
     print('gpu part: ' + json.dumps(out), file=sys.stderr, flush=True)
     if ws == 1 and not args.no_cpu_baseline:
         v, gates, secs, info, th = cpu_layer(w, args.cpu_budget, threads=os.cpu_count())
         out['cpu_baseline'] = {'value': v, 'unit': 'gates/s', 'cores': th, 'kind': 'port',
-                               'sample': f'steady-state layer 1 ({gates} gates) of the same circuit on the CPU oracle '
-                                         f'(torch CPU, exact SVD), {info["extrapolated_svd_steps"]} of '
+                               'sample': f'steady-state layer 1 ({gates} gates) of the seed-0 circuit on the CPU '
+                                         f'oracle (torch CPU, exact SVD), {info["extrapolated_svd_steps"]} of '
                                          f'{info["extrapolated_svd_steps"] + info["measured_svd_steps"]} SVD-sweep '
                                          f'steps extrapolated from measured ones; est. {secs:.1f} s per layer'}
     print(json.dumps(out), flush=True)

@@ -146,6 +146,54 @@ mpdo_status mpdo_expect_ops(mpdo_chain_t ch, const int *sites, const double *ops
 mpdo_status mpdo_expect_pauli_batch(mpdo_chain_t ch, const int8_t *paulis, int nterms,
                                     double *out);
 
+/* ---- Batched evolution of independent circuits ----------------------------
+ * A batch runner owns `workers` host threads, each with its own engine (its
+ * own non-blocking stream and memory pool) on `device`.  mpdo_batch_run hands
+ * whole circuits to the workers, longest first, so that the small
+ * factorisation launches of many circuits overlap on the GPU.  Each circuit
+ * runs the same path as mpdo_chain_create + mpdo_apply_* + mpdo_truncate, so
+ * its result does not depend on the worker or on the other circuits.  There
+ * is no counterpart in the reference (its callers loop over circuits). */
+typedef struct mpdo_batch_s *mpdo_batch_t;
+
+enum { MPDO_OP_1Q = 1, MPDO_OP_2Q = 2, MPDO_OP_TRUNCATE = 3, MPDO_OP_KAPPA = 4 };
+
+typedef struct {
+  int n;                     /* qubits */
+  int dtype;                 /* MPDO_C64 / MPDO_C128 */
+  int connected;             /* as mpdo_chain_create */
+  const double *vectors;     /* n x 2 complex initial product state */
+  int chi, kappa;            /* truncate(): <= 0 means no cap */
+  double max_err;            /* < 0: no error rule */
+  int noisy;                 /* truncate() runs the kappa pass */
+  double abs_cutoff;         /* 2q split cutoff (GLOBAL_MINIMUM in the reference) */
+  int nops;
+  const int *op_kind;        /* MPDO_OP_* per op */
+  const int *op_site;        /* 1q: site; 2q: the smaller site of the pair */
+  const int *op_k;           /* Kraus count (1q: 4K doubles, 2q: 16K complex) */
+  const int64_t *op_offset;  /* start of each op's tensor in `kraus`, in doubles */
+  const double *kraus;       /* interleaved complex, layouts as mpdo_apply_1q / _2q */
+  double *z;                 /* out (nullable): n values <Z_i> */
+  double *zz;                /* out (nullable): n-1 values <Z_i Z_{i+1}> */
+  double *discarded;         /* out (nullable): (number of truncate ops) x (n-1) weights */
+} mpdo_program;
+
+mpdo_status mpdo_batch_create(int device, int workers, mpdo_batch_t *out);
+mpdo_status mpdo_batch_destroy(mpdo_batch_t b);
+/* Applies mpdo_engine_set_option to every worker's engine. */
+mpdo_status mpdo_batch_set_option(mpdo_batch_t b, const char *name, double value);
+mpdo_status mpdo_batch_num_workers(mpdo_batch_t b, int *workers);
+/* The engine of one worker (for readouts of chains returned by a run). */
+mpdo_status mpdo_batch_engine(mpdo_batch_t b, int worker, mpdo_engine_t *out);
+/* Runs every program to completion.  chains_out (nullable, ncirc): the final
+ * states, owned by the caller afterwards (mpdo_chain_destroy), each living on
+ * the engine of worker_out[i] (nullable).  status_out (nullable, ncirc): each
+ * circuit's status.  Returns the first failing circuit's status (all circuits
+ * are attempted); mpdo_batch_error gives each failure's message. */
+mpdo_status mpdo_batch_run(mpdo_batch_t b, int ncirc, const mpdo_program *progs, mpdo_chain_t *chains_out,
+                           int *worker_out, int *status_out);
+const char *mpdo_batch_error(mpdo_batch_t b, int circuit);
+
 /* Kernel-level test hooks (no counterpart in the reference).  Host in/out,
  * row-major complex (interleaved doubles).
  * mpdo_debug_qr:  A (m x n) = Q (m x k) R (k x n), k = min(m, n), Householder

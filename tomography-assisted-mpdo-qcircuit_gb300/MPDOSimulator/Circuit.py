@@ -80,9 +80,14 @@ class TensorCircuit(QuantumCircuit):
         key = None if (gate.variational or gate.name == 'ArbSingleGate') else gate.name
         if key is not None and key in self.noiseTensorDict:
             return self.noiseTensorDict[key]
-        t = torch.einsum('nlm, ljk, ji -> nimk', self.Noise.decayTensor.to(g.device),
-                         self.Noise.dephasingTensor.to(g.device), g.to(self.Noise.decayTensor.dtype))
-        t = self._np(t.reshape(2, 2, -1))
+        # einsum('nlm, ljk, ji -> nimk', decay, dephasing, G): the gate-free
+        # part is contracted once per pair of noise tensors
+        pre_key = (id(self.Noise.decayTensor), id(self.Noise.dephasingTensor))
+        if getattr(self, '_noise_pre_key', None) != pre_key:
+            self._noise_pre = np.einsum('nlm,ljk->njmk', self._np(self.Noise.decayTensor),
+                                        self._np(self.Noise.dephasingTensor))
+            self._noise_pre_key = pre_key
+        t = np.einsum('njmk,ji->nimk', self._noise_pre, self._np(g)).reshape(2, 2, -1)
         if key is not None:
             self.noiseTensorDict[key] = t
         return t
@@ -103,61 +108,70 @@ class TensorCircuit(QuantumCircuit):
             self.noiseTensorDict[key] = t
         return t
 
-    def _add_gate(self, chain, _layer_num: int, _oqs: List[int], _gate: Optional[QuantumGate] = None):
-        """Circuit.py:180-224."""
+    def _gate_ops(self, _layer_num: int, _oqs: List[int], _gate: Optional[QuantumGate] = None) -> list:
+        """Circuit.py:180-224: the engine operations of one gate layer,
+        ('1q', site, kraus[2,2,K]) per target or ('2q', site_min,
+        kraus[o_min,o_max,i_min,i_max,K])."""
         if not isinstance(_oqs, list):
             raise TypeError('Operating qubits must be a list.')
         if _oqs[0] is None:
-            return None
+            return []
         if max(_oqs) >= self.qnumber:
             raise ValueError(f'Qubit index out of range, max index is Q{max(_oqs)}.')
         gate = _gate or self.layers[_layer_num]
         if not gate or gate.name == 'MeasureZ':
-            return None
+            return []
         if not isinstance(gate, QuantumGate):
             raise TypeError(f'Gate must be a QuantumGate, current type is {type(gate)}.')
         if gate.single:
             t = self._noisy_1q(gate)
-            for q in _oqs:
-                chain.apply_1q(q, t)
-        else:
-            if len(_oqs) != 2 or _oqs[0] == _oqs[1]:
-                raise ValueError('Invalid operating qubits for a two-qubit gate.')
-            a, b = _oqs
-            if abs(a - b) != 1:
-                raise ValueError('Only nearest-neighbour two-qubit gates are supported by the MPDO engine.')
-            t = self._noisy_2q(gate)
-            if t.ndim == 4:
-                t = t[..., None]
-            if a > b:
-                t = np.transpose(t, (1, 0, 3, 2, 4))
-            chain.apply_2q(min(a, b), t, GLOBAL_MINIMUM)
+            return [('1q', q, t) for q in _oqs]
+        if len(_oqs) != 2 or _oqs[0] == _oqs[1]:
+            raise ValueError('Invalid operating qubits for a two-qubit gate.')
+        a, b = _oqs
+        if abs(a - b) != 1:
+            raise ValueError('Only nearest-neighbour two-qubit gates are supported by the MPDO engine.')
+        t = self._noisy_2q(gate)
+        if t.ndim == 4:
+            t = t[..., None]
+        if a > b:
+            t = np.transpose(t, (1, 0, 3, 2, 4))
+        return [('2q', min(a, b), t)]
 
-    def evolve(self, state: List[QubitNode]):
-        """Circuit.py:469-491."""
-        from mpdo_gb300 import Chain
+    def _add_gate(self, chain, _layer_num: int, _oqs: List[int], _gate: Optional[QuantumGate] = None):
+        """Circuit.py:180-224."""
+        for op in self._gate_ops(_layer_num, _oqs, _gate):
+            if op[0] == '1q':
+                chain.apply_1q(op[1], op[2])
+            else:
+                chain.apply_2q(op[1], op[2], GLOBAL_MINIMUM)
+
+    def _engine_ops(self) -> list:
+        """Every engine operation evolve() performs, in order (Circuit.py:469-491):
+        gate ops, ('truncate',) per truncate layer and a final ('kappa',) when
+        the last layer of a noisy circuit is not a truncate."""
+        ops, last = [], None
+        for i, layer in enumerate(self.layers):
+            name = layer.name.lower()
+            if 'truncate' in name:
+                ops.append(('truncate',))
+            elif 'barrier' not in name:
+                ops += self._gate_ops(i, self._oqs_list[i])
+            last = name
+        if not self.ideal and last is not None and 'truncate' not in last:          # Circuit.py:487-489
+            ops.append(('kappa',))
+        return ops
+
+    def _initial(self, state: List[QubitNode]):
         if len(state) != self.qnumber:
             raise ValueError('state length differs from the number of qubits')
         self._initState = [QubitNode(s.tensor.clone(), s.name, s.axis_names, s.connected) for s in state]
         vectors = np.stack([self._np(s.tensor).reshape(2) for s in state])
         connected = all(getattr(s, 'connected', False) for s in state)
         dt = 'complex128' if self.dtype == torch.complex128 else 'complex64'
-        chain = Chain(vectors, dtype=dt, connected=connected, engine=self._engine())
-        noisy = not self.ideal
-        self.discarded_weights = []
-        last = None
-        for i, layer in enumerate(self.layers):
-            name = layer.name.lower()
-            if 'truncate' in name:
-                d = chain.truncate(self.chi, self.kappa, self.max_truncation_err, noisy, report=True)
-                self.discarded_weights.append(d)
-            elif 'barrier' in name:
-                pass
-            else:
-                self._add_gate(chain, i, self._oqs_list[i])
-            last = name
-        if noisy and last is not None and 'truncate' not in last:          # Circuit.py:487-489
-            chain.kappa_truncate(self.kappa, self.max_truncation_err)
+        return vectors, connected, dt
+
+    def _attach_chain(self, chain, state: List[QubitNode]):
         self._chain = chain
         self._dm, self._dmNodes, self._vector = None, None, None
         nodes = [QubitNode(None, f'qubit_{k}', [f'bond_{k - 1}_{k}', f'physics_{k}', f'I_{k}', f'bond_{k}_{k + 1}'],
@@ -165,6 +179,26 @@ class TensorCircuit(QuantumCircuit):
         self._stateNodes = nodes
         state[:] = nodes
         return nodes
+
+    def evolve(self, state: List[QubitNode]):
+        """Circuit.py:469-491."""
+        from mpdo_gb300 import Chain
+        vectors, connected, dt = self._initial(state)
+        ops = self._engine_ops()
+        chain = Chain(vectors, dtype=dt, connected=connected, engine=self._engine())
+        noisy = not self.ideal
+        self.discarded_weights = []
+        for op in ops:
+            if op[0] == '1q':
+                chain.apply_1q(op[1], op[2])
+            elif op[0] == '2q':
+                chain.apply_2q(op[1], op[2], GLOBAL_MINIMUM)
+            elif op[0] == 'truncate':
+                self.discarded_weights.append(
+                    chain.truncate(self.chi, self.kappa, self.max_truncation_err, noisy, report=True))
+            else:
+                chain.kappa_truncate(self.kappa, self.max_truncation_err)
+        return self._attach_chain(chain, state)
 
     def forward(self, state):
         self.evolve(state)
@@ -288,3 +322,39 @@ class TensorCircuit(QuantumCircuit):
         return [self.sample(shots=shots_per_scheme, orientation=s, reduced=reduced, sample_string=False,
                             _tqdm_disable=True, _require_bool_result=_require_bool_result, _require_counts=False)
                 for s in measurement_schemes]
+
+
+def evolve_batch(circuits: List[TensorCircuit], states: Optional[List[List[QubitNode]]] = None,
+                 workers: int = 16) -> List[dict]:
+    """Evolve many independent circuits concurrently on one GPU (no
+    counterpart in the reference, whose callers loop over ``evolve``).
+
+    Each circuit ends exactly as after its own ``evolve(state)``: the same
+    engine operations run on one of ``workers`` engines (own stream and memory
+    pool each), and the circuit's state, ``discarded_weights`` and readouts
+    are attached to it.  ``states`` defaults to |0...0> for every circuit.
+    Returns per circuit dict(z=<Z_i>, zz=<Z_i Z_{i+1}>, discarded=per-bond
+    weights of every truncate layer), computed by the worker right after the
+    evolution (not normalised by Tr rho, as ``dmOperations.pauli_expect``)."""
+    from mpdo_gb300 import Batch
+    from .Tools import create_ket0Series
+    if not circuits:
+        return []
+    devs = {_cuda_index(c.device) for c in circuits}
+    if len(devs) != 1:
+        raise ValueError('all circuits of a batch must select the same CUDA device')
+    if states is None:
+        states = [create_ket0Series(c.qnumber, dtype=c.dtype) for c in circuits]
+    if len(states) != len(circuits):
+        raise ValueError('one initial state per circuit')
+    progs = []
+    for c, st in zip(circuits, states):
+        vectors, connected, dt = c._initial(st)
+        progs.append(dict(n=c.qnumber, dtype=dt, vectors=vectors, connected=connected, chi=c.chi, kappa=c.kappa,
+                          max_err=c.max_truncation_err, noisy=not c.ideal, cutoff=GLOBAL_MINIMUM,
+                          ops=c._engine_ops(), z=True, zz=True, discarded=True))
+    results = Batch.get(devs.pop(), workers).run(progs, keep_chains=True)
+    for c, st, r in zip(circuits, states, results):
+        c.discarded_weights = [row.copy() for row in r['discarded']]
+        c._attach_chain(r.pop('chain'), st)
+    return results

@@ -7,6 +7,6 @@ __version__ = '1.0.0'
 
 from . import Tools  # noqa: F401
 from . import dmOperations  # noqa: F401
-from .Circuit import TensorCircuit  # noqa: F401
+from .Circuit import TensorCircuit, evolve_batch  # noqa: F401
 
-__all__ = ['TensorCircuit', 'Tools', 'dmOperations']
+__all__ = ['TensorCircuit', 'Tools', 'dmOperations', 'evolve_batch']

@@ -5,6 +5,9 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
+#include <set>
+#include <utility>
 
 namespace mpdo {
 
@@ -84,6 +87,22 @@ template <typename T> inline View<T> view_adjoint_of_rowmajor(const cx<T> *p, in
 
 // Device status words written by factorisation kernels.
 enum DevStatus : int { DEV_OK = 0, DEV_NOT_CONVERGED = 1, DEV_NONFINITE = 2 };
+
+// Dynamic shared memory: every kernel that takes more than the default 48 KB
+// is opted in once per device to the one ceiling all its launches stay under
+// (200 KB), so host threads launching concurrently never change the limit
+// under each other's launches.
+constexpr int kSmemCeiling = 200 * 1024;
+inline void smem_optin_raw(const void *kernel) {
+  static std::mutex mu;
+  static std::set<std::pair<const void *, int>> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.insert({kernel, dev}).second)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemCeiling);
+}
+template <typename F> inline void smem_optin(F *kernel) { smem_optin_raw(reinterpret_cast<const void *>(kernel)); }
 
 // Launch counter (all kernels of this library go through count_launch()).
 void count_launch();

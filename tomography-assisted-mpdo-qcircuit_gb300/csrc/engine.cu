@@ -29,6 +29,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 namespace mpdo {
@@ -64,6 +65,13 @@ struct Engine {
   std::vector<ProfRec> recs;
   double acc_ms[8] = {0}, acc_flops[8] = {0}, acc_bytes[8] = {0};
   long long acc_n[8] = {0};
+  // Freed device blocks kept for reuse, by rounded size.  Every block of an
+  // engine is used on the engine's one stream, so a block freed after its
+  // last use was enqueued can serve the next allocation at once (stream order
+  // separates the uses); the driver's allocator is then off the hot path.
+  std::unordered_map<size_t, std::vector<void *>> cache;
+  std::unordered_map<void *, size_t> live;
+  size_t cached_bytes = 0;
 };
 
 // kernel classes reported by mpdo_engine_profile_read
@@ -97,18 +105,61 @@ static void prof_flush(Engine &e) {
   e.recs.clear();
 }
 
+// Allocation size classes: multiples of 256 B up to 64 KiB, then eight steps
+// per power of two (at most 12.5% slack).
+static size_t size_class(size_t bytes) {
+  if (bytes <= 65536) return (bytes + 255) / 256 * 256;
+  int k = 63 - __builtin_clzll((unsigned long long)(bytes - 1));   // 2^k < bytes <= 2^(k+1)
+  const size_t step = size_t(1) << (k - 2);
+  return (bytes + step - 1) / step * step;
+}
+
+static constexpr size_t kCacheCapBytes = size_t(16) << 30;   // per engine
+
+static void release_cache(Engine &e) {
+  for (auto &kv : e.cache)
+    for (void *q : kv.second) cudaFreeAsync(q, e.stream);
+  e.cache.clear();
+  e.cached_bytes = 0;
+}
+
 static void *dalloc(Engine &e, size_t bytes) {
   if (bytes == 0) bytes = 16;
+  const size_t sz = size_class(bytes);
+  auto it = e.cache.find(sz);
+  if (it != e.cache.end() && !it->second.empty()) {
+    void *p = it->second.back();
+    it->second.pop_back();
+    e.cached_bytes -= sz;
+    e.live[p] = sz;
+    return p;
+  }
   void *p = nullptr;
-  cudaError_t err = cudaMallocFromPoolAsync(&p, bytes, e.pool, e.stream);
+  cudaError_t err = cudaMallocFromPoolAsync(&p, sz, e.pool, e.stream);
   if (err != cudaSuccess) {
     cudaGetLastError();
-    fail(MPDO_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(err));
+    release_cache(e);                        // give cached blocks back and retry once
+    err = cudaMallocFromPoolAsync(&p, sz, e.pool, e.stream);
+    if (err != cudaSuccess) {
+      cudaGetLastError();
+      fail(MPDO_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(err));
+    }
   }
+  e.live[p] = sz;
   return p;
 }
 static void dfree(Engine &e, void *p) {
-  if (p) MPDO_CUDA_CHECK(cudaFreeAsync(p, e.stream));
+  if (!p) return;
+  auto it = e.live.find(p);
+  if (it == e.live.end()) {                  // not from dalloc: hand straight back
+    cudaFreeAsync(p, e.stream);
+    return;
+  }
+  const size_t sz = it->second;
+  e.live.erase(it);
+  e.cache[sz].push_back(p);
+  e.cached_bytes += sz;
+  if (e.cached_bytes > kCacheCapBytes) release_cache(e);
 }
 
 // Scoped device buffer
@@ -128,7 +179,7 @@ template <typename X> struct DBuf {
   }
   X *release() { X *q = p; p = nullptr; return q; }
   void reset() { if (p && e) dfree(*e, p); p = nullptr; }
-  ~DBuf() { if (p && e) { cudaFreeAsync(p, e->stream); } }
+  ~DBuf() { if (p && e) dfree(*e, p); }
 };
 
 static int *status_slot(Engine &e, int count);
@@ -1114,6 +1165,7 @@ mpdo_status mpdo_engine_destroy(mpdo_engine_t eng) {
     if (!eng) return;
     Engine &e = eng->e;
     cudaSetDevice(e.device);
+    release_cache(e);
     cudaStreamSynchronize(e.stream);
     if (e.d_status) cudaFree(e.d_status);
     if (e.pool) cudaMemPoolDestroy(e.pool);
@@ -1225,7 +1277,7 @@ mpdo_status mpdo_chain_destroy(mpdo_chain_t ch) {
     if (!ch) return;
     set_device(ch->eng);
     for (auto &s : ch->s)
-      if (s.p) cudaFreeAsync(s.p, ch->eng->e.stream);
+      if (s.p) dfree(ch->eng->e, s.p);
     delete ch;
   });
 }

@@ -178,7 +178,7 @@ void jacobi_svd(cudaStream_t st, int batch, int m, int n, const View<T> &in, cx<
   if (n > 1024) return;  // callers never ask for more columns
   size_t bytes = ((size_t)m * n + (wout ? (size_t)n * n : 0)) * sizeof(cx<T>);
   if (bytes <= SMEM_CAP) {
-    cudaFuncSetAttribute(k_jacobi<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    smem_optin(k_jacobi<T, true>);
     k_jacobi<T, true><<<batch, JT, bytes, st>>>(m, n, in, uout, sigma, wout, xws, wws, max_sweeps, tol, status);
   } else {
     k_jacobi<T, false><<<batch, JT, 0, st>>>(m, n, in, uout, sigma, wout, xws, wws, max_sweeps, tol, status);
@@ -298,7 +298,7 @@ void bjacobi_round(cudaStream_t st, int m, int n, int bs, int nblk, cx<T> *X, co
                    int npairs, const T *gmax2, int inner_sweeps, int *flag) {
   const T tol = T(4) * sqrt(T(std::max(m, 1))) * Eps<T>::v;
   const size_t bytes = (size_t)m * 2 * bs * sizeof(cx<T>);
-  cudaFuncSetAttribute(k_bjacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  smem_optin(k_bjacobi<T>);
   k_bjacobi<T><<<npairs, 512, bytes, st>>>(m, n, bs, nblk, X, pairs_round, tol, gmax2, inner_sweeps, flag);
   count_launch();
 }

@@ -226,7 +226,7 @@ void qr_factor_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const 
                       cx<T> *tau, cx<T> *rstack) {
   const size_t bytes = (size_t)mc * n * sizeof(cx<T>);
   if (bytes <= SMEM_CAP) {
-    cudaFuncSetAttribute(k_qr_factor<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    smem_optin(k_qr_factor<T, true>);
     k_qr_factor<T, true><<<nchunks, QR_NT, bytes, st>>>(m, n, mc, in, vws, tau, rstack);
   } else {
     k_qr_factor<T, false><<<nchunks, QR_NT, 0, st>>>(m, n, mc, in, vws, tau, rstack);
@@ -239,11 +239,11 @@ void qr_apply_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const c
                      const cx<T> *bin, int64_t ldb, int nq, cx<T> *qout, int64_t ldq) {
   const size_t bytes = ((size_t)mc + (size_t)mc * nq) * sizeof(cx<T>);
   if (bytes <= SMEM_CAP) {
-    cudaFuncSetAttribute(k_qr_apply<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    smem_optin(k_qr_apply<T, true>);
     k_qr_apply<T, true><<<nchunks, QR_NT, bytes, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
   } else {
     const size_t vb = (size_t)mc * sizeof(cx<T>);
-    cudaFuncSetAttribute(k_qr_apply<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vb);
+    smem_optin(k_qr_apply<T, false>);
     k_qr_apply<T, false><<<nchunks, QR_NT, vb, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
   }
   count_launch();

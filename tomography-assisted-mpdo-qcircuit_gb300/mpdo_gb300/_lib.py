@@ -27,6 +27,17 @@ _D = C.c_double
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
 
+MPDO_OP_1Q, MPDO_OP_2Q, MPDO_OP_TRUNCATE, MPDO_OP_KAPPA = 1, 2, 3, 4
+
+
+class Program(C.Structure):
+    """``mpdo_program`` of include/mpdo_gb300.h (one circuit of a batch run)."""
+    _fields_ = [('n', C.c_int), ('dtype', C.c_int), ('connected', C.c_int), ('vectors', _DP),
+                ('chi', C.c_int), ('kappa', C.c_int), ('max_err', C.c_double), ('noisy', C.c_int),
+                ('abs_cutoff', C.c_double), ('nops', C.c_int), ('op_kind', _IP), ('op_site', _IP),
+                ('op_k', _IP), ('op_offset', C.POINTER(C.c_int64)), ('kraus', _DP), ('z', _DP), ('zz', _DP),
+                ('discarded', _DP)]
+
 # name -> (restype, argtypes); mirrors include/mpdo_gb300.h
 SIGNATURES = {
     'mpdo_abi_version': (_I, []),
@@ -60,6 +71,13 @@ SIGNATURES = {
     'mpdo_debug_svd': (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_debug_split': (_I, [_P, _I, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_right_svd_noalloc': (_I, [_I, _I, _P, _P, _P, _P, _P]),
+    'mpdo_batch_create': (_I, [_I, _I, C.POINTER(_P)]),
+    'mpdo_batch_destroy': (_I, [_P]),
+    'mpdo_batch_set_option': (_I, [_P, C.c_char_p, _D]),
+    'mpdo_batch_num_workers': (_I, [_P, _IP]),
+    'mpdo_batch_engine': (_I, [_P, _I, C.POINTER(_P)]),
+    'mpdo_batch_run': (_I, [_P, _I, C.POINTER(Program), C.POINTER(_P), _IP, _IP]),
+    'mpdo_batch_error': (C.c_char_p, [_P, _I]),
 }
 
 _lock = threading.Lock()

@@ -221,3 +221,117 @@ class Chain:
         check(self._lib.mpdo_expect_pauli_batch(self.handle, codes.ctypes.data_as(C.POINTER(C.c_int8)),
                                                 codes.shape[0], _dptr(out)))
         return out
+
+
+class Batch:
+    """Independent circuits run concurrently (``mpdo_batch_*``): ``workers``
+    host threads, each with its own engine (stream + memory pool) on one
+    device, take whole circuits longest first.  ``run`` takes host programs
+    and returns per-circuit readouts and, optionally, the final chains."""
+
+    _cache: Dict[tuple, 'Batch'] = {}
+
+    def __init__(self, device: int = 0, workers: int = 16):
+        self._lib = load()
+        h = C.c_void_p()
+        check(self._lib.mpdo_batch_create(int(device), int(workers), C.byref(h)))
+        self.handle = h
+        self.device = int(device)
+        n = C.c_int()
+        check(self._lib.mpdo_batch_num_workers(self.handle, C.byref(n)))
+        self.workers = n.value
+        self.engines = []
+        for w in range(self.workers):
+            eh = C.c_void_p()
+            check(self._lib.mpdo_batch_engine(self.handle, w, C.byref(eh)))
+            e = Engine.__new__(Engine)
+            e._lib, e.handle, e.device, e._owner = self._lib, eh, self.device, self
+            self.engines.append(e)
+
+    @classmethod
+    def get(cls, device: int = 0, workers: int = 16) -> 'Batch':
+        key = (int(device), int(workers))
+        if key not in cls._cache:
+            cls._cache[key] = cls(device, workers)
+        return cls._cache[key]
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h is not None and h.value:
+            try:
+                self._lib.mpdo_batch_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def set_option(self, name: str, value: float) -> None:
+        check(self._lib.mpdo_batch_set_option(self.handle, name.encode(), float(value)))
+
+    def run(self, programs: Sequence[dict], keep_chains: bool = False):
+        """Each program: dict(n, dtype ('complex64'|'complex128'), vectors (n x 2),
+        connected, chi, kappa, max_err, noisy, cutoff, ops, z, zz, discarded)
+        with ops a list of ('1q', site, kraus[2,2,K]) / ('2q', site_min,
+        kraus[o_min,o_max,i_min,i_max,K]) / ('truncate',) / ('kappa',).
+        Returns one dict per program: z, zz, discarded (as requested) and
+        chain (when keep_chains)."""
+        kinds = {'1q': _lib.MPDO_OP_1Q, '2q': _lib.MPDO_OP_2Q, 'truncate': _lib.MPDO_OP_TRUNCATE,
+                 'kappa': _lib.MPDO_OP_KAPPA}
+        arr = (_lib.Program * max(1, len(programs)))()
+        alive, outs = [], []
+        for i, p in enumerate(programs):
+            n = int(p['n'])
+            ops = p['ops']
+            kind = np.array([kinds[o[0]] for o in ops], dtype=np.int32)
+            site = np.array([o[1] if len(o) > 1 else 0 for o in ops], dtype=np.int32)
+            tens = [np.ascontiguousarray(np.asarray(o[2], dtype=np.complex128)) if len(o) > 2 else None for o in ops]
+            kk = np.array([t.shape[-1] if t is not None and t.ndim in (3, 5) else 1 for t in tens], dtype=np.int32)
+            sizes = [2 * t.size if t is not None else 0 for t in tens]
+            off = np.zeros(len(ops), dtype=np.int64)
+            if len(ops) > 1:
+                off[1:] = np.cumsum(sizes[:-1])
+            flat = np.concatenate([t.view(np.float64).ravel() for t in tens if t is not None]) \
+                if any(t is not None for t in tens) else np.zeros(1)
+            vec = _cplx(np.asarray(p['vectors'], dtype=np.complex128).reshape(n, 2))
+            ntr = int(sum(1 for o in ops if o[0] == 'truncate'))
+            o = {'z': np.zeros(n) if p.get('z') else None, 'zz': np.zeros(max(n - 1, 1)) if p.get('zz') else None,
+                 'discarded': np.zeros(max(ntr * (n - 1), 1)) if p.get('discarded') else None}
+            max_err = p.get('max_err')
+            pr = arr[i]
+            pr.n, pr.connected = n, int(bool(p.get('connected', False)))
+            pr.dtype = _lib.MPDO_C128 if str(p.get('dtype', 'complex64')).endswith('128') else _lib.MPDO_C64
+            pr.vectors = _dptr(vec)
+            pr.chi, pr.kappa = int(p.get('chi') or 0), int(p.get('kappa') or 0)
+            pr.max_err = -1.0 if max_err is None else float(max_err)
+            pr.noisy = int(bool(p.get('noisy', False)))
+            pr.abs_cutoff = float(p.get('cutoff', 2.718281828459045e-8))
+            pr.nops = len(ops)
+            pr.op_kind = kind.ctypes.data_as(C.POINTER(C.c_int))
+            pr.op_site = site.ctypes.data_as(C.POINTER(C.c_int))
+            pr.op_k = kk.ctypes.data_as(C.POINTER(C.c_int))
+            pr.op_offset = off.ctypes.data_as(C.POINTER(C.c_int64))
+            pr.kraus = _dptr(flat)
+            pr.z = _dptr(o['z']) if o['z'] is not None else None
+            pr.zz = _dptr(o['zz']) if o['zz'] is not None else None
+            pr.discarded = _dptr(o['discarded']) if o['discarded'] is not None else None
+            alive += [kind, site, kk, off, flat, vec]
+            outs.append((o, n, ntr, pr.dtype))
+        nc = len(programs)
+        chains = (C.c_void_p * max(1, nc))()
+        workers = (C.c_int * max(1, nc))()
+        status = (C.c_int * max(1, nc))()
+        st = self._lib.mpdo_batch_run(self.handle, nc, arr, chains if keep_chains else None, workers, status)
+        results = []
+        for i, (o, n, ntr, dt) in enumerate(outs):
+            r = {'status': int(status[i]), 'worker': int(workers[i])}
+            if o['z'] is not None:
+                r['z'] = o['z'][:n]
+            if o['zz'] is not None:
+                r['zz'] = o['zz'][:n - 1]
+            if o['discarded'] is not None:
+                r['discarded'] = o['discarded'][:ntr * (n - 1)].reshape(ntr, n - 1)
+            if keep_chains and chains[i]:
+                r['chain'] = Chain(None, 'complex128' if dt == _lib.MPDO_C128 else 'complex64',
+                                   engine=self.engines[int(workers[i])], _handle=C.c_void_p(chains[i]))
+            results.append(r)
+        check(st)
+        return results
