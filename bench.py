@@ -286,7 +286,7 @@ def _sum_profiles(profs):
     out = {}
     for p in profs:
         for k, v in p.items():
-            if k == 'wide_bonds':
+            if k in ('wide_bonds', 'phases'):
                 continue
             o = out.setdefault(k, dict(launches=0, ms=0.0, flops=0.0, bytes=0.0))
             for f in o:
@@ -338,6 +338,7 @@ def gpu_arm(args):
     plain_prof = eng.profile_read()
     eng.profile(False)
     plain_wide = plain_prof.pop('wide_bonds')
+    plain_phases = plain_prof.pop('phases')
     t0 = time.perf_counter()
     circuit.evolve(S.Tools.create_ket0Series(w.n, dtype=cdt, connected=True))
     marg = circuit.probabilities([0])
@@ -351,6 +352,7 @@ def gpu_arm(args):
              'kernel_breakdown_ms': {k: {'launches': v['launches'], 'ms': round(v['ms'], 3)}
                                      for k, v in plain_prof.items() if v['launches']},
              'wide_bond_svd': plain_wide,
+             'phases_ms': {k: round(v['ms'], 1) for k, v in plain_phases.items()},
              'discarded_weight': {'per_bond_max': max((float(d.max()) for d in dw if d.size), default=None),
                                   'last_truncation_sum': float(dw[-1].sum()) if dw else None,
                                   'truncations': len(dw)},
@@ -365,6 +367,7 @@ def gpu_arm(args):
     torch.cuda.synchronize()
     barrier(ws)
     launches0 = eng.launch_count()
+    hist0 = eng.launch_histogram()
     step_ms = []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -378,6 +381,8 @@ def gpu_arm(args):
             step_ms.append(a.elapsed_time(b))
     barrier(ws)
     launches = eng.launch_count() - launches0
+    hist1 = eng.launch_histogram()
+    by_launcher = {k: (v - hist0.get(k, 0)) // args.steps for k, v in hist1.items() if v - hist0.get(k, 0)}
     clocks = clk.summary()
     total_ms = allreduce_max(sum(step_ms), ws)
     value = ws * B * gates_per_circuit * args.steps / (total_ms / 1e3)
@@ -422,7 +427,9 @@ def gpu_arm(args):
            'e2e': {'value': e2e_value, 'unit': 'gates/s', 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': d2h,
                    'ms_per_step': e2e_total / len(e2e_ms),
                    'path': 'MPDOSimulator.evolve_batch on TensorCircuit objects built per step'},
-           'gpu_launches': int(launches), 'clocks': clocks, 'roofline': _roofline(bprof, peaks),
+           'gpu_launches': int(launches),
+           'gpu_launches_per_step_by_launcher': dict(sorted(by_launcher.items(), key=lambda kv: -kv[1])),
+           'clocks': clocks, 'roofline': _roofline(bprof, peaks),
            'kernel_breakdown_ms': {k: {'launches': v['launches'], 'ms': round(v['ms'], 3)}
                                    for k, v in bprof.items() if v['launches']},
            'wide_bond_svd': wide, 'z_first_circuit': z0,

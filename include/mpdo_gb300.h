@@ -84,15 +84,21 @@ mpdo_status mpdo_engine_sync(mpdo_engine_t eng);
  * every launch is bracketed by CUDA events on the engine stream and its
  * algorithmic flop and byte counts are accumulated.  Classes: 0 GEMM,
  * 1 Householder QR factor, 2 QR explicit-Q apply, 3 one-sided Jacobi,
- * 4 Kraus 1q apply, 5 two-site gate mix, 6 other.  Class 7 returns counters
+ * 4 Kraus 1q apply, 5 two-site gate mix, 6 other, 8 block-Jacobi rounds of
+ * wide bonds (class 3 is the single-CTA Jacobi).  Class 7 returns counters
  * instead: launches = wide bonds solved by the range finder, flops = wide
  * bonds solved by the exact block Jacobi, bytes = the largest accepted relative
- * residual |Y - Q Q^H Y|_F / |Y|_F.  Enabling resets the sums. */
+ * residual |Y - Q Q^H Y|_F / |Y|_F.  Classes 9-12 are phases (launches =
+ * count, ms = summed span): 9 QR sweep, 10 SVD sweep, 11 kappa pass, 12 the
+ * wide-bond SVDs inside the SVD sweep.  Enabling resets the sums. */
 mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable);
 mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *launches, double *ms,
                                      double *flops, double *bytes);
-/* Number of kernels this engine launched so far. */
+/* Number of kernels this library launched so far (all engines). */
 mpdo_status mpdo_engine_launch_count(mpdo_engine_t eng, uint64_t *count);
+/* Launches so far per launcher function, as text lines "name count\n"
+ * (truncated to len-1 characters). */
+mpdo_status mpdo_launch_histogram(char *buf, int len);
 
 /* Product state.  vectors: n x 2 complex (4n doubles).  connected != 0 adds
  * dimension-1 bonds between all neighbours (the reference's check_connected

@@ -148,3 +148,13 @@ def test_split_wide_range_matches_exact(eng, dtype):
         eng.set_option('wide_range', -1)
     tol = 1e-11 if dtype == 'complex128' else 2e-5
     np.testing.assert_allclose(L1 @ R1, L0 @ R0, atol=tol * np.abs(L0 @ R0).max() * 10)
+
+
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-4)])
+def test_split_wide_512(eng, dtype, tol):
+    # the pair bond at chi=128 (Mr = 512): Gram 512 x 512 through block Jacobi
+    y = _decaying(512, 2048, 9, 0.02)
+    L, R = eng.debug_split(y, 128, dtype)
+    u, s, vh = np.linalg.svd(y, full_matrices=False)
+    best = (u[:, :128] * s[:128]) @ vh[:128]
+    np.testing.assert_allclose(L @ R, best, atol=tol * s[0] * 10)

@@ -104,9 +104,12 @@ inline void smem_optin_raw(const void *kernel) {
 }
 template <typename F> inline void smem_optin(F *kernel) { smem_optin_raw(reinterpret_cast<const void *>(kernel)); }
 
-// Launch counter (all kernels of this library go through count_launch()).
-void count_launch();
+// Launch counter (all kernels of this library go through count_launch(),
+// which also keeps a count per launcher function).
+void count_launch(const char *fn = __builtin_FUNCTION());
 uint64_t launch_count();
+// (launcher name, launches) pairs so far; returns how many were written.
+int launch_histogram(const char **names, uint64_t *counts, int cap);
 
 }  // namespace mpdo
 

@@ -63,8 +63,8 @@ struct Engine {
   struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };
   bool profiling = false;
   std::vector<ProfRec> recs;
-  double acc_ms[8] = {0}, acc_flops[8] = {0}, acc_bytes[8] = {0};
-  long long acc_n[8] = {0};
+  double acc_ms[13] = {0}, acc_flops[13] = {0}, acc_bytes[13] = {0};
+  long long acc_n[13] = {0};
   // Freed device blocks kept for reuse, by rounded size.  Every block of an
   // engine is used on the engine's one stream, so a block freed after its
   // last use was enqueued can serve the next allocation at once (stream order
@@ -75,7 +75,13 @@ struct Engine {
 };
 
 // kernel classes reported by mpdo_engine_profile_read
-enum KClass { K_GEMM = 0, K_QR_FACTOR = 1, K_QR_APPLY = 2, K_JACOBI = 3, K_KRAUS1Q = 4, K_MIX2Q = 5, K_OTHER = 6 };
+enum KClass {
+  K_GEMM = 0, K_QR_FACTOR = 1, K_QR_APPLY = 2, K_JACOBI = 3, K_KRAUS1Q = 4, K_MIX2Q = 5, K_OTHER = 6,
+  K_BJACOBI = 8,  // (7 reports the wide-bond counters)
+  // phases (spans of many launches, overlapping the kernel classes)
+  P_QR_SWEEP = 9, P_SVD_SWEEP = 10, P_KAPPA = 11, P_WIDE_SVD = 12
+};
+constexpr int kProfClasses = 13;
 
 // Launch wrapper: when profiling, bracket the launch with events and keep the
 // algorithmic flop/byte count of the call.
@@ -104,6 +110,23 @@ static void prof_flush(Engine &e) {
   }
   e.recs.clear();
 }
+
+// Phase span (profiling only): events around a block of launches.
+struct Phase {
+  Engine &e;
+  Engine::ProfRec r;
+  Phase(Engine &eng, int cls) : e(eng), r{cls, nullptr, nullptr, 0, 0} {
+    if (!e.profiling) return;
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, e.stream);
+  }
+  ~Phase() {
+    if (!e.profiling || !r.a) return;
+    cudaEventRecord(r.b, e.stream);
+    e.recs.push_back(r);
+  }
+};
 
 // Allocation size classes: multiples of 256 B up to 64 KiB, then eight steps
 // per power of two (at most 12.5% slack).
@@ -379,7 +402,7 @@ static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
     MPDO_CUDA_CHECK(cudaMemsetAsync(flag.p, 0, sizeof(int), e.stream));
     const double fl = 4.0 * (4.0 * m * (double)n * n) / std::max(1, rounds);
     for (int r = 0; r < rounds; ++r)
-      prof(e, K_JACOBI, fl, (double)esz * m * n * 2, [&] {
+      prof(e, K_BJACOBI, fl, (double)esz * m * n * 2, [&] {
         bjacobi_round<T>(e.stream, m, n, bs, nblk, X, dp.p + (size_t)r * np * 2, np, gmax.p, 2, flag.p);
       });
     MPDO_CUDA_CHECK(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
@@ -511,6 +534,7 @@ static bool left_svd_wide_range(Engine &e, const cx<T> *Y, int Mr, int Nc, int w
 template <typename T>
 static void left_svd_wide(Engine &e, const cx<T> *Y, int Mr, int Nc, int want, DBuf<cx<T>> &U, DBuf<T> &s,
                           int &kr) {
+  Phase ph(e, P_WIDE_SVD);
   const bool try_range = e.wide_range > 0 || (e.wide_range < 0 && sizeof(T) == 8);
   if (try_range && left_svd_wide_range<T>(e, Y, Mr, Nc, want, U, s, kr)) {
     e.wide_range_hits++;
@@ -659,6 +683,7 @@ template <typename T> static void apply_2q(mpdo_chain_s *ch, int i, const double
 // TNNOptimizer.py:87-108, with pending pairs fused (see file header)
 template <typename T> static void qr_sweep(mpdo_chain_s *ch) {
   Engine &e = ch->eng->e;
+  Phase ph(e, P_QR_SWEEP);
   const int n = ch->n;
   DBuf<cx<T>> Rprev;
   int Rrows = 0, Rcols = 0;
@@ -733,6 +758,7 @@ template <typename T> static void qr_sweep(mpdo_chain_s *ch) {
 // TNNOptimizer.py:111-134
 template <typename T> static void svd_sweep(mpdo_chain_s *ch, int chi, double max_err, double *wdev) {
   Engine &e = ch->eng->e;
+  Phase ph(e, P_SVD_SWEEP);
   for (int idx = ch->n - 1; idx >= 1; --idx) {
     const Site P = ch->s[idx - 1], S = ch->s[idx];
     const int b = S.l, Nc = 2 * S.a * S.r;
@@ -763,6 +789,7 @@ template <typename T> static void svd_sweep(mpdo_chain_s *ch, int chi, double ma
 // Jacobi on R.
 template <typename T> static void kappa_pass(mpdo_chain_s *ch, int kappa, double max_err) {
   Engine &e = ch->eng->e;
+  Phase ph(e, P_KAPPA);
   if (kappa <= 0 && max_err < 0) return;
   for (int i = 0; i < ch->n; ++i) {
     const Site s = ch->s[i];
@@ -1200,7 +1227,7 @@ mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable) {
     need(eng != nullptr, "engine is NULL");
     Engine &e = eng->e;
     prof_flush(e);
-    for (int c = 0; c < 8; ++c) { e.acc_ms[c] = e.acc_flops[c] = e.acc_bytes[c] = 0; e.acc_n[c] = 0; }
+    for (int c = 0; c < kProfClasses; ++c) { e.acc_ms[c] = e.acc_flops[c] = e.acc_bytes[c] = 0; e.acc_n[c] = 0; }
     e.wide_range_hits = e.wide_exact_calls = 0;
     e.wide_resid_max = 0;
     e.profiling = enable != 0;
@@ -1211,7 +1238,7 @@ mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *l
                                      double *bytes) {
   return guard([&] {
     need(eng && launches && ms && flops && bytes, "NULL argument");
-    need(kclass >= 0 && kclass < 8, "kernel class out of range");
+    need(kclass >= 0 && kclass < kProfClasses, "kernel class out of range");
     Engine &e = eng->e;
     prof_flush(e);
     if (kclass == 7) {   // wide-bond SVD path counters: range finder accepted / exact block Jacobi
@@ -1248,6 +1275,19 @@ mpdo_status mpdo_engine_launch_count(mpdo_engine_t eng, uint64_t *count) {
   return guard([&] {
     need(eng != nullptr && count != nullptr, "NULL argument");
     *count = launch_count();
+  });
+}
+
+mpdo_status mpdo_launch_histogram(char *buf, int len) {
+  return guard([&] {
+    need(buf != nullptr && len > 0, "buffer is NULL");
+    const char *names[128];
+    uint64_t counts[128];
+    const int n = launch_histogram(names, counts, 128);
+    std::string out;
+    for (int i = 0; i < n; ++i) out += std::string(names[i]) + " " + std::to_string(counts[i]) + "\n";
+    std::strncpy(buf, out.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
   });
 }
 

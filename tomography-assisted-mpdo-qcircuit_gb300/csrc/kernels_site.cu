@@ -8,8 +8,45 @@
 namespace mpdo {
 
 static std::atomic<uint64_t> g_launches{0};
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// Per-launcher counts: a lock-free open-addressing table keyed by the
+// launcher's function-name literal (pointer identity).
+constexpr int kHistSlots = 128;
+static std::atomic<const char *> g_hist_key[kHistSlots];
+static std::atomic<uint64_t> g_hist_count[kHistSlots];
+
+void count_launch(const char *fn) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  const uintptr_t h = reinterpret_cast<uintptr_t>(fn);
+  for (int i = 0; i < kHistSlots; ++i) {
+    const int slot = (int)((h / 8 + (uintptr_t)i) % kHistSlots);
+    const char *k = g_hist_key[slot].load(std::memory_order_acquire);
+    if (k == nullptr) {
+      const char *expected = nullptr;
+      if (g_hist_key[slot].compare_exchange_strong(expected, fn) || expected == fn) {
+        g_hist_count[slot].fetch_add(1, std::memory_order_relaxed);
+        return;
+      }
+      continue;
+    }
+    if (k == fn) {
+      g_hist_count[slot].fetch_add(1, std::memory_order_relaxed);
+      return;
+    }
+  }
+}
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+int launch_histogram(const char **names, uint64_t *counts, int cap) {
+  int n = 0;
+  for (int i = 0; i < kHistSlots && n < cap; ++i) {
+    const char *k = g_hist_key[i].load(std::memory_order_acquire);
+    if (k) {
+      names[n] = k;
+      counts[n] = g_hist_count[i].load(std::memory_order_relaxed);
+      ++n;
+    }
+  }
+  return n;
+}
 
 namespace {
 inline int nblocks(int64_t n, int t = 256) { return (int)std::min<int64_t>((n + t - 1) / t, 152 * 32); }

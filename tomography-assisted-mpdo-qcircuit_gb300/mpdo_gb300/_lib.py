@@ -51,6 +51,7 @@ SIGNATURES = {
     'mpdo_engine_profile': (_I, [_P, _I]),
     'mpdo_engine_profile_read': (_I, [_P, _I, C.POINTER(C.c_longlong), _DP, _DP, _DP]),
     'mpdo_engine_launch_count': (_I, [_P, C.POINTER(C.c_uint64)]),
+    'mpdo_launch_histogram': (_I, [C.c_char_p, _I]),
     'mpdo_chain_create': (_I, [_P, _I, _I, _DP, _I, C.POINTER(_P)]),
     'mpdo_chain_destroy': (_I, [_P]),
     'mpdo_chain_clone': (_I, [_P, C.POINTER(_P)]),

@@ -78,21 +78,43 @@ class Engine:
                                          m, n, int(keep), _dptr(_cplx(y)), _dptr(lo), _dptr(ro)))
         return lo.view(np.complex128).reshape(m, keep), ro.view(np.complex128).reshape(keep, n)
 
-    KERNEL_CLASSES = ('gemm', 'qr_factor', 'qr_apply', 'jacobi', 'kraus1q', 'mix2q', 'other')
+    KERNEL_CLASSES = ('gemm', 'qr_factor', 'qr_apply', 'jacobi', 'kraus1q', 'mix2q', 'other', None, 'bjacobi')
+    PHASES = ('qr_sweep', 'svd_sweep', 'kappa_pass', 'wide_svd')
 
     def profile(self, enable: bool) -> None:
         check(self._lib.mpdo_engine_profile(self.handle, int(bool(enable))))
 
     def profile_read(self) -> dict:
-        """{class: dict(launches, ms, flops, bytes)} accumulated since profile(True)."""
+        """{class: dict(launches, ms, flops, bytes)} accumulated since profile(True),
+        plus 'wide_bonds' (range finder / exact counts) and 'phases' ({phase:
+        dict(count, ms)} for the QR sweep, SVD sweep, kappa pass and the
+        wide-bond SVDs inside the SVD sweep)."""
         out = {}
         for i, name in enumerate(self.KERNEL_CLASSES):
+            if name is None:
+                continue
             n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
             check(self._lib.mpdo_engine_profile_read(self.handle, i, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
             out[name] = dict(launches=int(n.value), ms=ms.value, flops=fl.value, bytes=by.value)
         n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
         check(self._lib.mpdo_engine_profile_read(self.handle, 7, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
         out['wide_bonds'] = dict(range_finder=int(n.value), exact=int(fl.value), max_residual=by.value)
+        phases = {}
+        for i, name in enumerate(self.PHASES, start=9):
+            n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
+            check(self._lib.mpdo_engine_profile_read(self.handle, i, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
+            phases[name] = dict(count=int(n.value), ms=ms.value)
+        out['phases'] = phases
+        return out
+
+    def launch_histogram(self) -> Dict[str, int]:
+        """Kernel launches so far per launcher function (all engines)."""
+        buf = C.create_string_buffer(1 << 16)
+        check(self._lib.mpdo_launch_histogram(buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt = line.rsplit(' ', 1)
+            out[name] = int(cnt)
         return out
 
     def launch_count(self) -> int:

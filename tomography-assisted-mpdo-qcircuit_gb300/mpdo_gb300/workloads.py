@@ -72,6 +72,21 @@ def config1(n: int = 32, depth: int = 20, chi: int = 64, kappa: int = 4, seed: i
                     layers, depth=depth)
 
 
+def config2(seed: int) -> Workload:
+    """One circuit of the uneven batch: n ~ U{12..40}, depth ~ U{10..30},
+    chi from {16, 32, 64, 128}, kappa from {2, 4}, drawn from
+    torch.Generator seed ``seed``; gates and noise as the n=32 workload (its
+    angles and gate picks continue from the same generator's seed)."""
+    g = torch.Generator().manual_seed(int(seed))
+    n = int(torch.randint(12, 41, (1,), generator=g))
+    depth = int(torch.randint(10, 31, (1,), generator=g))
+    chi = (16, 32, 64, 128)[int(torch.randint(0, 4, (1,), generator=g))]
+    kappa = (2, 4)[int(torch.randint(0, 2, (1,), generator=g))]
+    w = config1(n=n, depth=depth, chi=chi, kappa=kappa, seed=int(seed))
+    w.name = f'uneven batch circuit seed={seed}: n={n} depth={depth} chi={chi} kappa={kappa}'
+    return w
+
+
 def amplitude_damping(gamma: float) -> np.ndarray:
     k = np.array([[[1, 0], [0, math.sqrt(1 - gamma)]], [[0, math.sqrt(gamma)], [0, 0]]], dtype=np.complex128)
     return np.transpose(k, (1, 2, 0))
