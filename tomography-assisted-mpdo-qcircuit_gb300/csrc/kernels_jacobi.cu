@@ -92,15 +92,12 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
         if (a >= n || c >= n) continue;
         const int pc = min(a, c), qc = max(a, c);
         cx<T> *xp = X + (int64_t)pc * m, *xq = X + (int64_t)qc * m;
-        T al = T(0), be = T(0);
+        // squared norms carried from the sweep start through the rotations
+        // (alpha' = alpha - t|g|, beta' = beta + t|g|): one reduction per pair
+        const T al = nrm[pc], be = nrm[qc];
         cx<T> ga = czero<T>();
-        for (int i = lane; i < m; i += 32) {
-          const cx<T> u = xp[i], v = xq[i];
-          al += cabs2<T>(u);
-          be += cabs2<T>(v);
-          cfmac<T>(ga, u, v);
-        }
-        al = wsum(al); be = wsum(be); ga.x = wsum(ga.x); ga.y = wsum(ga.y);
+        for (int i = lane; i < m; i += 32) cfmac<T>(ga, xp[i], xq[i]);
+        ga.x = wsum(ga.x); ga.y = wsum(ga.y);
         const T g = sqrt(cabs2<T>(ga));
         if (!(g > tol * sqrt(al * be)) || al <= floor_abs || be <= floor_abs || al <= Eps<T>::tiny ||
             be <= Eps<T>::tiny || g <= Eps<T>::tiny)
@@ -112,6 +109,11 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
         // e = gamma/|gamma|; x_p' = c x_p - s conj(e) x_q ; x_q' = s x_p + c conj(e) x_q
         const cx<T> ec = cmk<T>(ga.x / g, -ga.y / g);
         const cx<T> sec = cscale<T>(ec, sn), cec = cscale<T>(ec, cs);
+        __syncwarp();
+        if (lane == 0) {
+          nrm[pc] = fmax(al - t * g, T(0));
+          nrm[qc] = be + t * g;
+        }
         for (int i = lane; i < m; i += 32) {
           const cx<T> u = xp[i], v = xq[i];
           const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
@@ -217,46 +219,69 @@ __global__ void __launch_bounds__(512) k_bjacobi(int m, int n, int bs, int nblk,
   const T floor_abs = (*gmax2) * T(16) * T(n) * Eps<T>::v * Eps<T>::v;
   const int ne = nc + (nc & 1);
   const int npairs = ne / 2;
+  // squared column norms, recomputed at the start of every inner sweep and
+  // carried through rotations exactly as the 2 x 2 Gram's diagonal moves
+  // (alpha' = alpha - t|g|, beta' = beta + t|g|), so a pair costs one
+  // reduction (its inner product) instead of three
+  __shared__ T nrm2[64];
+  auto rotate_pair = [&](int pc, int qc) -> bool {
+    cx<T> *xp = S + (int64_t)pc * m, *xq = S + (int64_t)qc * m;
+    cx<T> ga = czero<T>();
+    for (int i = lane; i < m; i += 32) cfmac<T>(ga, xp[i], xq[i]);
+    ga.x = wsum(ga.x); ga.y = wsum(ga.y);
+    const T al = nrm2[pc], be = nrm2[qc];
+    const T g = sqrt(cabs2<T>(ga));
+    if (!(g > tol * sqrt(al * be)) || al <= floor_abs || be <= floor_abs || al <= Eps<T>::tiny ||
+        be <= Eps<T>::tiny || g <= Eps<T>::tiny)
+      return false;
+    const T zeta = (be - al) / (T(2) * g);
+    const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+    const T cs = T(1) / sqrt(T(1) + t * t);
+    const T sn = cs * t;
+    const cx<T> ec = cmk<T>(ga.x / g, -ga.y / g);
+    const cx<T> sec = cscale<T>(ec, sn), cec = cscale<T>(ec, cs);
+    __syncwarp();
+    for (int i = lane; i < m; i += 32) {
+      const cx<T> u = xp[i], v = xq[i];
+      const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
+      xp[i] = cmk<T>(cs * u.x - ev_s.x, cs * u.y - ev_s.y);
+      xq[i] = cmk<T>(sn * u.x + ev_c.x, sn * u.y + ev_c.y);
+    }
+    if (lane == 0) {
+      nrm2[pc] = fmax(al - t * g, T(0));
+      nrm2[qc] = be + t * g;
+    }
+    return true;
+  };
+  // after the first inner sweep (all pairs) only the pairs that straddle the
+  // two blocks are revisited: bs steps of bs disjoint pairs
+  const bool cross_only_ok = (w0 == w1) && w0 > 0;
   for (int sw = 0; sw < inner_sweeps && nc >= 2; ++sw) {
     if (tid == 0) rot_count = 0;
+    for (int j = warp; j < nc; j += nw) {
+      T sq = T(0);
+      for (int i = lane; i < m; i += 32) sq += cabs2<T>(S[(int64_t)j * m + i]);
+      sq = wsum(sq);
+      if (lane == 0) nrm2[j] = sq;
+    }
     __syncthreads();
-    for (int r = 0; r < ne - 1; ++r) {
-      for (int p = warp; p < npairs; p += nw) {
-        int a, c;
-        if (p == 0) { a = ne - 1; c = r; }
-        else { a = (r + p) % (ne - 1); c = (r - p + ne - 1) % (ne - 1); }
-        if (a >= nc || c >= nc) continue;
-        // only pairs that straddle the two blocks need work after the first sweep
-        const int pc = min(a, c), qc = max(a, c);
-        cx<T> *xp = S + (int64_t)pc * m, *xq = S + (int64_t)qc * m;
-        T al = T(0), be = T(0);
-        cx<T> ga = czero<T>();
-        for (int i = lane; i < m; i += 32) {
-          const cx<T> u = xp[i], v = xq[i];
-          al += cabs2<T>(u);
-          be += cabs2<T>(v);
-          cfmac<T>(ga, u, v);
+    if (sw == 0 || !cross_only_ok) {
+      for (int r = 0; r < ne - 1; ++r) {
+        for (int p = warp; p < npairs; p += nw) {
+          int a, c;
+          if (p == 0) { a = ne - 1; c = r; }
+          else { a = (r + p) % (ne - 1); c = (r - p + ne - 1) % (ne - 1); }
+          if (a >= nc || c >= nc) continue;
+          if (rotate_pair(min(a, c), max(a, c)) && lane == 0) atomicAdd(&rot_count, 1);
         }
-        al = wsum(al); be = wsum(be); ga.x = wsum(ga.x); ga.y = wsum(ga.y);
-        const T g = sqrt(cabs2<T>(ga));
-        if (!(g > tol * sqrt(al * be)) || al <= floor_abs || be <= floor_abs || al <= Eps<T>::tiny ||
-            be <= Eps<T>::tiny || g <= Eps<T>::tiny)
-          continue;
-        const T zeta = (be - al) / (T(2) * g);
-        const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-        const T cs = T(1) / sqrt(T(1) + t * t);
-        const T sn = cs * t;
-        const cx<T> ec = cmk<T>(ga.x / g, -ga.y / g);
-        const cx<T> sec = cscale<T>(ec, sn), cec = cscale<T>(ec, cs);
-        for (int i = lane; i < m; i += 32) {
-          const cx<T> u = xp[i], v = xq[i];
-          const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
-          xp[i] = cmk<T>(cs * u.x - ev_s.x, cs * u.y - ev_s.y);
-          xq[i] = cmk<T>(sn * u.x + ev_c.x, sn * u.y + ev_c.y);
-        }
-        if (lane == 0) atomicAdd(&rot_count, 1);
+        __syncthreads();
       }
-      __syncthreads();
+    } else {
+      for (int st = 0; st < w0; ++st) {
+        for (int i = warp; i < w0; i += nw)
+          if (rotate_pair(i, w0 + (i + st) % w0) && lane == 0) atomicAdd(&rot_count, 1);
+        __syncthreads();
+      }
     }
     const int rc = rot_count;
     __syncthreads();

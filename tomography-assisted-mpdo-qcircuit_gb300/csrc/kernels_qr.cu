@@ -63,12 +63,29 @@ __device__ T block_max(T v, T *red) {
   return red[32];
 }
 
+// Scaled 2-norm parts of x[i0..rows) by one warp: amax = max |re|, |im|
+// and q = sum |x_i / amax|^2 (q = 0 when amax is below the smallest normal).
+template <typename T>
+__device__ __forceinline__ void warp_col_norm(const cx<T> *x, int i0, int rows, int lane, T &amax, T &q) {
+  T pmax = T(0);
+  for (int i = i0 + lane; i < rows; i += 32) pmax = fmax(pmax, fmax(fabs(x[i].x), fabs(x[i].y)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pmax = fmax(pmax, __shfl_xor_sync(0xffffffffu, pmax, o));
+  T part = T(0);
+  if (pmax >= NormalMin<T>::v) {
+    const T inv = T(1) / pmax;
+    for (int i = i0 + lane; i < rows; i += 32) part += cabs2<T>(cscale<T>(x[i], inv));
+  }
+  amax = pmax;
+  q = warp_sum(part);
+}
+
 template <typename T, bool SMEM>
 __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<T> in, cx<T> *vws,
                                                      cx<T> *tau_out, cx<T> *rstack) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T red[33];
   __shared__ cx<T> hh[2];  // tau, scale
+  __shared__ T cn[2];      // scaled norm parts of the next column
   const int c = blockIdx.x;
   const int r0 = c * mc;
   const int rows = min(mc, m - r0);
@@ -84,29 +101,36 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
   }
   __syncthreads();
 
+  // Column j's reflector needs the scaled 2-norm of its part below the
+  // diagonal (as LAPACK's nrm2: max |x_i|, then sum (|x_i| / max)^2, so that
+  // columns near the underflow threshold keep an exact norm and the
+  // reflector stays unitary).  The warp that applies reflector j to column
+  // j+1 computes that column's norm right after its update, so each column
+  // costs two block barriers: one after the reflector is formed, one after
+  // the trailing update.  The reflector's vector v = scl * x is used unscaled
+  // in the update (the factors fold into the coefficients) and scaled in
+  // place one step later.
+  if (warp == 0 && kc > 0) {
+    T a, q;
+    warp_col_norm<T>(W + 0 * ld, 1, rows, lane, a, q);
+    if (lane == 0) { cn[0] = a; cn[1] = q; }
+  }
+  __syncthreads();
+  cx<T> prev_tau = czero<T>(), prev_scl = czero<T>();
   for (int j = 0; j < kc; ++j) {
-    // scaled 2-norm of the column below the diagonal (as LAPACK's nrm2):
-    // max |x_i| first, then sum (|x_i| / max)^2, so that columns near the
-    // underflow threshold keep an exact norm and the reflector stays unitary
-    T pmax = T(0);
-    for (int i = j + 1 + tid; i < rows; i += blockDim.x) {
-      const cx<T> v = W[j * ld + i];
-      pmax = fmax(pmax, fmax(fabs(v.x), fabs(v.y)));
-    }
-    T amax = block_max(pmax, red);
+    T amax = cn[0];
+    const T xs = cn[1];
     // entries below the smallest normal number are underflow debris: the
     // column is treated as exactly zero (1/amax would overflow)
-    if (amax < NormalMin<T>::v) {
-      if (amax > T(0))
-        for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = czero<T>();
-      amax = T(0);
+    const bool debris = amax < NormalMin<T>::v;
+    if (debris && amax > T(0))
+      for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = czero<T>();
+    if (debris) amax = T(0);
+    if (j > 0) {          // deferred: v of reflector j-1
+      const bool id = prev_tau.x == T(0) && prev_tau.y == T(0);
+      for (int i = j + tid; i < rows; i += blockDim.x)
+        W[(j - 1) * ld + i] = id ? czero<T>() : cmul<T>(W[(j - 1) * ld + i], prev_scl);
     }
-    T part = T(0);
-    if (amax > T(0)) {
-      const T inv = T(1) / amax;
-      for (int i = j + 1 + tid; i < rows; i += blockDim.x) part += cabs2<T>(cscale<T>(W[j * ld + i], inv));
-    }
-    const T xs = block_sum(part, red);
     if (tid == 0) {
       const cx<T> al = W[j * ld + j];
       cx<T> tau = czero<T>(), scl = czero<T>();
@@ -128,25 +152,36 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
     }
     __syncthreads();
     const cx<T> tau = hh[0], scl = hh[1];
-    if (tau.x == T(0) && tau.y == T(0)) {
-      // H = I: v below the diagonal must read as zero
-      for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = czero<T>();
-      __syncthreads();
-      continue;
-    }
-    for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = cmul<T>(W[j * ld + i], scl);
-    __syncthreads();
-    const cx<T> ctau = cconj<T>(tau);
+    const bool ident = tau.x == T(0) && tau.y == T(0);
+    const cx<T> ctau = cconj<T>(tau), cscl = cconj<T>(scl);
     for (int k = j + 1 + warp; k < n; k += nw) {
-      cx<T> w = (lane == 0) ? W[k * ld + j] : czero<T>();
-      for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(w, W[j * ld + i], W[k * ld + i]);
-      w.x = warp_sum(w.x); w.y = warp_sum(w.y);
-      w = cmul<T>(ctau, w);
-      if (lane == 0) W[k * ld + j] = csub<T>(W[k * ld + j], w);
-      for (int i = j + 1 + lane; i < rows; i += 32) {
-        W[k * ld + i] = csub<T>(W[k * ld + i], cmul<T>(W[j * ld + i], w));
+      cx<T> *Wk = W + k * ld;
+      if (!ident) {
+        cx<T> d = czero<T>();
+        for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(d, W[j * ld + i], Wk[i]);
+        d.x = warp_sum(d.x); d.y = warp_sum(d.y);
+        // w = tau^H (W[j][k] + v^H W[:, k]) with v = scl x
+        const cx<T> w = cmul<T>(ctau, cadd<T>(Wk[j], cmul<T>(cscl, d)));
+        const cx<T> g = cmul<T>(scl, w);
+        __syncwarp();
+        if (lane == 0) Wk[j] = csub<T>(Wk[j], w);
+        for (int i = j + 1 + lane; i < rows; i += 32) Wk[i] = csub<T>(Wk[i], cmul<T>(W[j * ld + i], g));
+      }
+      if (k == j + 1 && k < kc) {
+        __syncwarp();
+        T a, q;
+        warp_col_norm<T>(Wk, k + 1, rows, lane, a, q);
+        if (lane == 0) { cn[0] = a; cn[1] = q; }
       }
     }
+    __syncthreads();
+    prev_tau = tau;
+    prev_scl = scl;
+  }
+  if (kc > 0) {           // v of the last reflector
+    const bool id = prev_tau.x == T(0) && prev_tau.y == T(0);
+    for (int i = kc + tid; i < rows; i += blockDim.x)
+      W[(kc - 1) * ld + i] = id ? czero<T>() : cmul<T>(W[(kc - 1) * ld + i], prev_scl);
     __syncthreads();
   }
   for (int j = kc; j < n; ++j) {
@@ -202,13 +237,35 @@ __global__ void __launch_bounds__(QR_NT) k_qr_apply(int m, int n, int mc, const 
     if (tj.x == T(0) && tj.y == T(0)) continue;
     for (int i = j + 1 + tid; i < rows; i += blockDim.x) vcol[i] = V[(int64_t)j * mc + i];
     __syncthreads();
-    for (int q = warp; q < nq; q += nw) {
-      cx<T> w = (lane == 0) ? B(j, q) : czero<T>();
-      for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(w, vcol[i], B(i, q));
-      w.x = warp_sum(w.x); w.y = warp_sum(w.y);
-      w = cmul<T>(tj, w);
-      if (lane == 0) B(j, q) = csub<T>(B(j, q), w);
-      for (int i = j + 1 + lane; i < rows; i += 32) B(i, q) = csub<T>(B(i, q), cmul<T>(vcol[i], w));
+    // each warp takes up to QB columns at a time, so every v_i read from
+    // shared memory serves QB products
+    constexpr int QB = 4;
+    for (int q0 = warp * QB; q0 < nq; q0 += nw * QB) {
+      const int nb = min(QB, nq - q0);
+      cx<T> w[QB];
+#pragma unroll
+      for (int b = 0; b < QB; ++b) w[b] = (lane == 0 && b < nb) ? B(j, q0 + b) : czero<T>();
+      for (int i = j + 1 + lane; i < rows; i += 32) {
+        const cx<T> v = vcol[i];
+#pragma unroll
+        for (int b = 0; b < QB; ++b)
+          if (b < nb) cfmac<T>(w[b], v, B(i, q0 + b));
+      }
+#pragma unroll
+      for (int b = 0; b < QB; ++b) {
+        w[b].x = warp_sum(w[b].x);
+        w[b].y = warp_sum(w[b].y);
+        w[b] = cmul<T>(tj, w[b]);
+      }
+      __syncwarp();
+      if (lane == 0)
+        for (int b = 0; b < nb; ++b) B(j, q0 + b) = csub<T>(B(j, q0 + b), w[b]);
+      for (int i = j + 1 + lane; i < rows; i += 32) {
+        const cx<T> v = vcol[i];
+#pragma unroll
+        for (int b = 0; b < QB; ++b)
+          if (b < nb) B(i, q0 + b) = csub<T>(B(i, q0 + b), cmul<T>(v, w[b]));
+      }
     }
     __syncthreads();
   }
