@@ -291,12 +291,13 @@ static void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
   int curm = m;
   while (true) {
     // chunk rows: the whole matrix if it fits in shared memory, else the
-    // largest multiple of 32 that fits (with the explicit-Q pass) and exceeds
+    // largest multiple of 32 that fits (with the explicit-Q pass and its two
+    // reflector buffers) and exceeds
     // n, so that every level shrinks the stacked R; else one global chunk
     int mc;
-    if ((size_t)curm * n * esz <= cap) mc = curm;
+    if ((size_t)curm * (n + 2) * esz <= cap) mc = curm;
     else {
-      size_t mcs = cap / ((size_t)(n + 1) * esz);
+      size_t mcs = cap / ((size_t)(n + 2) * esz);
       mcs = mcs / 32 * 32;
       mc = (mcs > (size_t)n) ? (int)std::min<size_t>(mcs, (size_t)curm) : curm;
     }

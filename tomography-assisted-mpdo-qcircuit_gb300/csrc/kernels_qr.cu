@@ -14,7 +14,7 @@
 namespace mpdo {
 
 namespace {
-constexpr int QR_NT = 512;
+constexpr int QR_NT = 1024;
 constexpr size_t SMEM_CAP = 200 * 1024;
 
 template <typename T>
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
                                                      cx<T> *tau_out, cx<T> *rstack) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ cx<T> hh[2];  // tau, scale
-  __shared__ T cn[2];      // scaled norm parts of the next column
+  __shared__ T cn[4];      // scaled norm parts of the next column, by parity
   const int c = blockIdx.x;
   const int r0 = c * mc;
   const int rows = min(mc, m - r0);
@@ -105,35 +105,36 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
   // diagonal (as LAPACK's nrm2: max |x_i|, then sum (|x_i| / max)^2, so that
   // columns near the underflow threshold keep an exact norm and the
   // reflector stays unitary).  The warp that applies reflector j to column
-  // j+1 computes that column's norm right after its update, so each column
-  // costs two block barriers: one after the reflector is formed, one after
-  // the trailing update.  The reflector's vector v = scl * x is used unscaled
-  // in the update (the factors fold into the coefficients) and scaled in
-  // place one step later.
+  // j+1 computes that column's norm right after its update (double-buffered
+  // by parity), every thread then forms reflector j+1 itself from that norm
+  // and the diagonal entry, and the writes that finish reflector j (beta on
+  // the diagonal, v = scl * x below it) are deferred to step j+1, where
+  // nothing reads column j.  One block barrier per column.
   if (warp == 0 && kc > 0) {
     T a, q;
     warp_col_norm<T>(W + 0 * ld, 1, rows, lane, a, q);
     if (lane == 0) { cn[0] = a; cn[1] = q; }
   }
   __syncthreads();
-  cx<T> prev_tau = czero<T>(), prev_scl = czero<T>();
+  cx<T> prev_tau = czero<T>(), prev_scl = czero<T>(), prev_beta = czero<T>();
+  bool prev_zero_v = false, prev_set_beta = false;
+  auto finish = [&](int jc) {            // deferred writes of reflector jc
+    for (int i = jc + 1 + tid; i < rows; i += blockDim.x)
+      W[jc * ld + i] = prev_zero_v ? czero<T>() : cmul<T>(W[jc * ld + i], prev_scl);
+    if (tid == 0 && prev_set_beta) W[jc * ld + jc] = prev_beta;
+  };
   for (int j = 0; j < kc; ++j) {
-    T amax = cn[0];
-    const T xs = cn[1];
+    if (j > 0) finish(j - 1);
+    T amax = cn[2 * (j & 1)];
+    const T xs = cn[2 * (j & 1) + 1];
     // entries below the smallest normal number are underflow debris: the
     // column is treated as exactly zero (1/amax would overflow)
     const bool debris = amax < NormalMin<T>::v;
-    if (debris && amax > T(0))
-      for (int i = j + 1 + tid; i < rows; i += blockDim.x) W[j * ld + i] = czero<T>();
     if (debris) amax = T(0);
-    if (j > 0) {          // deferred: v of reflector j-1
-      const bool id = prev_tau.x == T(0) && prev_tau.y == T(0);
-      for (int i = j + tid; i < rows; i += blockDim.x)
-        W[(j - 1) * ld + i] = id ? czero<T>() : cmul<T>(W[(j - 1) * ld + i], prev_scl);
-    }
-    if (tid == 0) {
-      const cx<T> al = W[j * ld + j];
-      cx<T> tau = czero<T>(), scl = czero<T>();
+    const cx<T> al = W[j * ld + j];
+    cx<T> tau = czero<T>(), scl = czero<T>(), beta_c = czero<T>();
+    bool set_beta = false;
+    {
       const T xnorm = amax * sqrt(xs);
       const T nrm = hypot(hypot(al.x, al.y), xnorm);
       if (!(xnorm == T(0) && al.y == T(0)) && nrm >= NormalMin<T>::v) {
@@ -145,43 +146,44 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
         const cx<T> ds = cmk<T>(d.x / sc, d.y / sc);
         const T dd = cabs2<T>(ds);
         scl = cmk<T>(ds.x / (dd * sc), -ds.y / (dd * sc));
-        W[j * ld + j] = cmk<T>(beta, T(0));
+        beta_c = cmk<T>(beta, T(0));
+        set_beta = true;
       }
-      hh[0] = tau; hh[1] = scl;
-      tau_out[(int64_t)c * n + j] = tau;
     }
-    __syncthreads();
-    const cx<T> tau = hh[0], scl = hh[1];
+    if (tid == 0) tau_out[(int64_t)c * n + j] = tau;
     const bool ident = tau.x == T(0) && tau.y == T(0);
     const cx<T> ctau = cconj<T>(tau), cscl = cconj<T>(scl);
     for (int k = j + 1 + warp; k < n; k += nw) {
       cx<T> *Wk = W + k * ld;
       if (!ident) {
         cx<T> d = czero<T>();
-        for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(d, W[j * ld + i], Wk[i]);
+        if (!debris)
+          for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(d, W[j * ld + i], Wk[i]);
         d.x = warp_sum(d.x); d.y = warp_sum(d.y);
         // w = tau^H (W[j][k] + v^H W[:, k]) with v = scl x
         const cx<T> w = cmul<T>(ctau, cadd<T>(Wk[j], cmul<T>(cscl, d)));
         const cx<T> g = cmul<T>(scl, w);
         __syncwarp();
         if (lane == 0) Wk[j] = csub<T>(Wk[j], w);
-        for (int i = j + 1 + lane; i < rows; i += 32) Wk[i] = csub<T>(Wk[i], cmul<T>(W[j * ld + i], g));
+        if (!debris)
+          for (int i = j + 1 + lane; i < rows; i += 32) Wk[i] = csub<T>(Wk[i], cmul<T>(W[j * ld + i], g));
       }
       if (k == j + 1 && k < kc) {
         __syncwarp();
         T a, q;
         warp_col_norm<T>(Wk, k + 1, rows, lane, a, q);
-        if (lane == 0) { cn[0] = a; cn[1] = q; }
+        if (lane == 0) { cn[2 * (k & 1)] = a; cn[2 * (k & 1) + 1] = q; }
       }
     }
     __syncthreads();
     prev_tau = tau;
     prev_scl = scl;
+    prev_beta = beta_c;
+    prev_set_beta = set_beta;
+    prev_zero_v = ident || debris;
   }
-  if (kc > 0) {           // v of the last reflector
-    const bool id = prev_tau.x == T(0) && prev_tau.y == T(0);
-    for (int i = kc + tid; i < rows; i += blockDim.x)
-      W[(kc - 1) * ld + i] = id ? czero<T>() : cmul<T>(W[(kc - 1) * ld + i], prev_scl);
+  if (kc > 0) {
+    finish(kc - 1);
     __syncthreads();
   }
   for (int j = kc; j < n; ++j) {
@@ -216,7 +218,7 @@ __global__ void __launch_bounds__(QR_NT) k_qr_apply(int m, int n, int mc, const 
   cx<T> *vcol = reinterpret_cast<cx<T> *>(smem_raw);
   // B: rows x nq; in shared memory column-major (ld = rows), else in place in
   // qout (row-major, leading dimension ldq)
-  cx<T> *Bs = vcol + mc;
+  cx<T> *Bs = vcol + 2 * mc;
   cx<T> *Bg = qout + (int64_t)r0 * ldq;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   auto B = [&](int i, int q) -> cx<T> & { return SMEM ? Bs[(int64_t)q * rows + i] : Bg[(int64_t)i * ldq + q]; };
@@ -232,39 +234,48 @@ __global__ void __launch_bounds__(QR_NT) k_qr_apply(int m, int n, int mc, const 
     B(i, q) = v;
   }
   __syncthreads();
+  // reflector j's vector is staged in vcol[j & 1] while reflector j+1 is
+  // being applied from the other buffer: one block barrier per reflector
+  auto stage = [&](int jj) {
+    cx<T> *vb = vcol + (jj & 1) * mc;
+    for (int i = jj + 1 + tid; i < rows; i += blockDim.x) vb[i] = V[(int64_t)jj * mc + i];
+  };
+  if (kc > 0) stage(kc - 1);
+  __syncthreads();
   for (int j = kc - 1; j >= 0; --j) {
+    if (j > 0) stage(j - 1);
     const cx<T> tj = tc[j];
-    if (tj.x == T(0) && tj.y == T(0)) continue;
-    for (int i = j + 1 + tid; i < rows; i += blockDim.x) vcol[i] = V[(int64_t)j * mc + i];
-    __syncthreads();
-    // each warp takes up to QB columns at a time, so every v_i read from
-    // shared memory serves QB products
-    constexpr int QB = 4;
-    for (int q0 = warp * QB; q0 < nq; q0 += nw * QB) {
-      const int nb = min(QB, nq - q0);
-      cx<T> w[QB];
+    const cx<T> *vj = vcol + (j & 1) * mc;
+    if (!(tj.x == T(0) && tj.y == T(0))) {
+      // each warp takes up to QB columns at a time, so every v_i read from
+      // shared memory serves QB products
+      constexpr int QB = 4;
+      for (int q0 = warp * QB; q0 < nq; q0 += nw * QB) {
+        const int nb = min(QB, nq - q0);
+        cx<T> w[QB];
 #pragma unroll
-      for (int b = 0; b < QB; ++b) w[b] = (lane == 0 && b < nb) ? B(j, q0 + b) : czero<T>();
-      for (int i = j + 1 + lane; i < rows; i += 32) {
-        const cx<T> v = vcol[i];
+        for (int b = 0; b < QB; ++b) w[b] = (lane == 0 && b < nb) ? B(j, q0 + b) : czero<T>();
+        for (int i = j + 1 + lane; i < rows; i += 32) {
+          const cx<T> v = vj[i];
 #pragma unroll
-        for (int b = 0; b < QB; ++b)
-          if (b < nb) cfmac<T>(w[b], v, B(i, q0 + b));
-      }
+          for (int b = 0; b < QB; ++b)
+            if (b < nb) cfmac<T>(w[b], v, B(i, q0 + b));
+        }
 #pragma unroll
-      for (int b = 0; b < QB; ++b) {
-        w[b].x = warp_sum(w[b].x);
-        w[b].y = warp_sum(w[b].y);
-        w[b] = cmul<T>(tj, w[b]);
-      }
-      __syncwarp();
-      if (lane == 0)
-        for (int b = 0; b < nb; ++b) B(j, q0 + b) = csub<T>(B(j, q0 + b), w[b]);
-      for (int i = j + 1 + lane; i < rows; i += 32) {
-        const cx<T> v = vcol[i];
+        for (int b = 0; b < QB; ++b) {
+          w[b].x = warp_sum(w[b].x);
+          w[b].y = warp_sum(w[b].y);
+          w[b] = cmul<T>(tj, w[b]);
+        }
+        __syncwarp();
+        if (lane == 0)
+          for (int b = 0; b < nb; ++b) B(j, q0 + b) = csub<T>(B(j, q0 + b), w[b]);
+        for (int i = j + 1 + lane; i < rows; i += 32) {
+          const cx<T> v = vj[i];
 #pragma unroll
-        for (int b = 0; b < QB; ++b)
-          if (b < nb) B(i, q0 + b) = csub<T>(B(i, q0 + b), cmul<T>(v, w[b]));
+          for (int b = 0; b < QB; ++b)
+            if (b < nb) B(i, q0 + b) = csub<T>(B(i, q0 + b), cmul<T>(v, w[b]));
+        }
       }
     }
     __syncthreads();
@@ -294,12 +305,12 @@ void qr_factor_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const 
 template <typename T>
 void qr_apply_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const cx<T> *vws, const cx<T> *tau,
                      const cx<T> *bin, int64_t ldb, int nq, cx<T> *qout, int64_t ldq) {
-  const size_t bytes = ((size_t)mc + (size_t)mc * nq) * sizeof(cx<T>);
+  const size_t bytes = ((size_t)2 * mc + (size_t)mc * nq) * sizeof(cx<T>);
   if (bytes <= SMEM_CAP) {
     smem_optin(k_qr_apply<T, true>);
     k_qr_apply<T, true><<<nchunks, QR_NT, bytes, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
   } else {
-    const size_t vb = (size_t)mc * sizeof(cx<T>);
+    const size_t vb = (size_t)2 * mc * sizeof(cx<T>);
     smem_optin(k_qr_apply<T, false>);
     k_qr_apply<T, false><<<nchunks, QR_NT, vb, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
   }
