@@ -75,6 +75,11 @@ mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
  *                outside its span is at rounding level, so the triplets are
  *                those of an exact SVD): 1 always, 0 never (Gram +
  *                block-Jacobi path only), -1 (default) complex128 only.
+ *   "wide_eig"   the exact wide-bond path diagonalises the Gram matrix by
+ *                Householder tridiagonalisation on a thread-block cluster +
+ *                bisection / inverse iteration (1), or by block Jacobi (0);
+ *                -1 (default): tridiagonal for complex128 only (in
+ *                complex64 it is less accurate than Jacobi on graded Grams).
  *   "max_sweeps" Jacobi sweep limit (default 60). */
 mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double value);
 /* Wait for all queued work; returns the first deferred device status
@@ -88,9 +93,11 @@ mpdo_status mpdo_engine_sync(mpdo_engine_t eng);
  * wide bonds (class 3 is the single-CTA Jacobi).  Class 7 returns counters
  * instead: launches = wide bonds solved by the range finder, flops = wide
  * bonds solved by the exact block Jacobi, bytes = the largest accepted relative
- * residual |Y - Q Q^H Y|_F / |Y|_F.  Classes 9-12 are phases (launches =
- * count, ms = summed span): 9 QR sweep, 10 SVD sweep, 11 kappa pass, 12 the
- * wide-bond SVDs inside the SVD sweep.  Enabling resets the sums. */
+ * residual |Y - Q Q^H Y|_F / |Y|_F, ms = wide bonds whose exact path used the
+ * tridiagonal eigensolver.  Classes 9-12 are phases (launches = count, ms =
+ * summed span): 9 QR sweep, 10 SVD sweep, 11 kappa pass, 12 the wide-bond
+ * SVDs inside the SVD sweep.  Class 13: cluster tridiagonalisation of
+ * wide-bond Gram matrices.  Enabling resets the sums. */
 mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable);
 mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *launches, double *ms,
                                      double *flops, double *bytes);

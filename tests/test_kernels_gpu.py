@@ -158,3 +158,32 @@ def test_split_wide_512(eng, dtype, tol):
     u, s, vh = np.linalg.svd(y, full_matrices=False)
     best = (u[:, :128] * s[:128]) @ vh[:128]
     np.testing.assert_allclose(L @ R, best, atol=tol * s[0] * 10)
+
+
+@pytest.mark.parametrize('m,n,keep,decay', [(128, 1024, 64, 0.03), (200, 1500, 80, 0.02), (256, 2048, 64, 0.01),
+                                            (256, 4096, 64, 0.003), (512, 2048, 128, 0.01)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-4)])
+def test_split_wide_tridiagonal_matches_jacobi(eng, m, n, keep, decay, dtype, tol):
+    # the exact wide path diagonalises the Gram by cluster tridiagonalisation
+    # (default) or block Jacobi; both must give the best rank-keep approximation
+    y = _decaying(m, n, m + keep, decay)
+    u, s, vh = np.linalg.svd(y, full_matrices=False)
+    best = (u[:, :keep] * s[:keep]) @ vh[:keep]
+    eng.profile(True)
+    try:
+        eng.set_option('wide_range', 0)
+        eng.set_option('wide_eig', 1)
+        L1, R1 = eng.debug_split(y, keep, dtype)
+        wide = eng.profile_read()['wide_bonds']
+        eng.set_option('wide_eig', 0)
+        L0, R0 = eng.debug_split(y, keep, dtype)
+    finally:
+        eng.set_option('wide_eig', -1)
+        eng.set_option('wide_range', -1)
+        eng.profile(False)
+    # (the cluster holds up to 512 rows in complex64, 374 in complex128)
+    assert wide['tridiagonal'] == (1 if m <= (512 if dtype == 'complex64' else 374) else 0)
+    np.testing.assert_allclose(L1 @ R1, best, atol=tol * s[0] * 10)
+    np.testing.assert_allclose(L0 @ R0, best, atol=tol * s[0] * 10)
+    g = L1.conj().T @ L1
+    np.testing.assert_allclose(np.diag(g).real, s[:keep], atol=tol * s[0])

@@ -55,6 +55,8 @@ struct Engine {
   int status_used = 0;
   bool fuse_2q = true;
   int wide_range = -1;              // verified range finder on wide bonds: 1 on, 0 off, -1 complex128 only
+  int wide_eig = -1;                // wide-bond Gram: tridiagonal eigensolver 1 on, 0 off, -1 complex128 only
+  long long wide_eig_calls = 0;
   long long wide_range_hits = 0, wide_exact_calls = 0;
   double wide_resid_max = 0;        // largest accepted |Y - Q Q^H Y|_F / |Y|_F
   int max_sweeps = 60;
@@ -63,8 +65,8 @@ struct Engine {
   struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };
   bool profiling = false;
   std::vector<ProfRec> recs;
-  double acc_ms[13] = {0}, acc_flops[13] = {0}, acc_bytes[13] = {0};
-  long long acc_n[13] = {0};
+  double acc_ms[14] = {0}, acc_flops[14] = {0}, acc_bytes[14] = {0};
+  long long acc_n[14] = {0};
   // Freed device blocks kept for reuse, by rounded size.  Every block of an
   // engine is used on the engine's one stream, so a block freed after its
   // last use was enqueued can serve the next allocation at once (stream order
@@ -79,9 +81,10 @@ enum KClass {
   K_GEMM = 0, K_QR_FACTOR = 1, K_QR_APPLY = 2, K_JACOBI = 3, K_KRAUS1Q = 4, K_MIX2Q = 5, K_OTHER = 6,
   K_BJACOBI = 8,  // (7 reports the wide-bond counters)
   // phases (spans of many launches, overlapping the kernel classes)
-  P_QR_SWEEP = 9, P_SVD_SWEEP = 10, P_KAPPA = 11, P_WIDE_SVD = 12
+  P_QR_SWEEP = 9, P_SVD_SWEEP = 10, P_KAPPA = 11, P_WIDE_SVD = 12,
+  K_HETRD = 13     // cluster tridiagonalisation of wide-bond Gram matrices
 };
-constexpr int kProfClasses = 13;
+constexpr int kProfClasses = 14;
 
 // Launch wrapper: when profiling, bracket the launch with events and keep the
 // algorithmic flop/byte count of the call.
@@ -412,7 +415,9 @@ static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
 }
 
 // Leading left singular vectors of a wide-bond Y (Mr x Nc): eigenvectors of
-// the Gram matrix Y Y^H by block Jacobi, then a Rayleigh-Ritz refinement in
+// the Gram matrix Y Y^H (Householder tridiagonalisation on a thread-block
+// cluster + bisection / inverse iteration for the top kr; block Jacobi where
+// the cluster does not fit), then a Rayleigh-Ritz refinement in
 // the leading kr = min(Mr, want + 16) directions (QR + one-sided Jacobi of
 // Z = U^H Y), which restores the accuracy of the small singular values.
 // U: Mr x kr column-major; s: Mr values (kr refined, the rest from the Gram).
@@ -427,19 +432,67 @@ static void left_svd_wide_exact(Engine &e, const cx<T> *Y, int Mr, int Nc, int w
     copy4d<T>(e.stream, X.p, G.p, d, st, 1);
   }
   G.reset();
-  block_jacobi<T>(e, Mr, Mr, X.p);
-  DBuf<cx<T>> Ua(e, (size_t)Mr * Mr), xws(e, (size_t)Mr * Mr);
-  DBuf<T> lam(e, Mr);
-  jacobi_svd<T>(e.stream, 1, Mr, Mr, CM<T>(X.p, Mr), Ua.p, lam.p, nullptr, xws.p, nullptr, 0, status_slot(e, 1));
-  X.reset();
-  xws.reset();
   kr = std::min(Mr, want + 16);
+  // leading kr eigenvectors of the Gram: U_a (Mr x kr, as a view) and the
+  // eigenvalue tail beyond them
+  DBuf<cx<T>> Ua;
+  View<T> ua_view{};
+  DBuf<T> lam, tail;
+  bool have = false;
+  // Measured against complex128 on the n=32, chi=64 circuit: the Gram's
+  // graded rounding keeps one-sided Jacobi accurate in single precision
+  // (|rho_2q error| 3e-5) while the tridiagonal route loses the small
+  // eigen-directions (1e-4 .. 3e-3, whether the reduction runs in single or
+  // double precision); in complex128 both agree to 1e-12 and the tridiagonal
+  // route is 1.8x faster.  Default: tridiagonal for complex128 only.
+  const bool use_eig = e.wide_eig > 0 || (e.wide_eig < 0 && sizeof(T) == 8);
+  if (use_eig && hetrd_cluster_fits<T>(Mr)) {
+    DBuf<T> dd(e, Mr), ee(e, Mr), work(e, (size_t)kr * 2 * Mr);
+    DBuf<cx<T>> vref(e, (size_t)(Mr - 1) * (Mr - 1)), tau(e, Mr), Zt(e, (size_t)Mr * kr);
+    lam = DBuf<T>(e, kr);
+    tail = DBuf<T>(e, 1);
+    cudaError_t err;
+    prof(e, K_HETRD, 16.0 / 3.0 * 4.0 * (double)Mr * Mr * Mr, (double)sizeof(cx<T>) * Mr * Mr * 2, [&] {
+      err = hetrd_cluster<T>(e.stream, Mr, X.p, dd.p, ee.p, vref.p, tau.p);
+    });
+    if (err == cudaSuccess) {
+      tridiag_top<T>(e.stream, Mr, dd.p, ee.p, kr, lam.p, Zt.p, work.p, tail.p);
+      const cx<T> *vr = vref.p, *ta = tau.p, *zt = Zt.p;
+      Ua = DBuf<cx<T>>(e, (size_t)Mr * kr);
+      // U = Q Z: row 0 is untouched by the reflectors, rows 1.. get Q'
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(Ua.p, zt, kr * sizeof(cx<T>), cudaMemcpyDeviceToDevice, e.stream));
+      prof(e, K_QR_APPLY, 8.0 * (double)Mr * Mr * kr, (double)sizeof(cx<T>) * ((double)Mr * Mr / 2 + 2.0 * Mr * kr), [&] {
+        qr_apply_chunks<T>(e.stream, Mr - 1, Mr - 1, Mr - 1, 1, vr, ta, zt + kr, kr, kr, Ua.p + kr, kr);
+      });
+      {  // to column-major, so the QR below reads it coalesced
+        DBuf<cx<T>> Uc(e, (size_t)Mr * kr);
+        const int64_t dd4[4] = {1, 1, kr, Mr};
+        const int64_t st4[4] = {0, 0, 1, kr};
+        copy4d<T>(e.stream, Uc.p, Ua.p, dd4, st4, 0);
+        Ua = std::move(Uc);
+      }
+      ua_view = CM<T>(Ua.p, Mr);
+      have = true;
+      e.wide_eig_calls++;
+    } else {
+      cudaGetLastError();          // the cluster could not be placed: Jacobi path
+    }
+  }
+  if (!have) {
+    block_jacobi<T>(e, Mr, Mr, X.p);
+    Ua = DBuf<cx<T>>(e, (size_t)Mr * Mr);
+    DBuf<cx<T>> xws(e, (size_t)Mr * Mr);
+    lam = DBuf<T>(e, Mr);
+    jacobi_svd<T>(e.stream, 1, Mr, Mr, CM<T>(X.p, Mr), Ua.p, lam.p, nullptr, xws.p, nullptr, 0, status_slot(e, 1));
+    ua_view = CM<T>(Ua.p, Mr);
+  }
+  X.reset();
   // Orthonormal basis of the leading kr eigenvector columns: directions with
   // rounding-level eigenvalues come out of the normalisation as arbitrary,
   // non-orthogonal vectors; Householder QR keeps the leading span and replaces
   // them by an orthonormal completion.
   DBuf<cx<T>> Qb(e, (size_t)Mr * kr), Rb(e, (size_t)kr * kr);
-  qr<T>(e, Mr, kr, CM<T>(Ua.p, Mr), Qb.p, Rb.p);                // Qb row-major Mr x kr
+  qr<T>(e, Mr, kr, ua_view, Qb.p, Rb.p);                         // Qb row-major Mr x kr
   Ua.reset();
   Rb.reset();
   DBuf<cx<T>> Z(e, (size_t)kr * Nc);
@@ -459,8 +512,16 @@ static void left_svd_wide_exact(Engine &e, const cx<T> *Y, int Mr, int Nc, int w
   s = DBuf<T>(e, Mr);
   MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p, sz.p, kr * sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
   if (Mr > kr) {
-    sqrt_inplace<T>(e.stream, lam.p, Mr);
-    MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p + kr, lam.p + kr, (Mr - kr) * sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
+    if (have) {
+      // only the energy of the rest of the spectrum is known: it goes to the
+      // first slot past kr (what the discarded-weight sums use)
+      MPDO_CUDA_CHECK(cudaMemsetAsync(s.p + kr, 0, (Mr - kr) * sizeof(T), e.stream));
+      sqrt_inplace<T>(e.stream, tail.p, 1);
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p + kr, tail.p, sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
+    } else {
+      sqrt_inplace<T>(e.stream, lam.p, Mr);
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(s.p + kr, lam.p + kr, (Mr - kr) * sizeof(T), cudaMemcpyDeviceToDevice, e.stream));
+    }
   }
 }
 
@@ -1218,6 +1279,7 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
     Engine &e = eng->e;
     if (k == "fuse_2q") e.fuse_2q = value != 0;
     else if (k == "wide_range") e.wide_range = value > 0 ? 1 : (value < 0 ? -1 : 0);
+    else if (k == "wide_eig") e.wide_eig = value > 0 ? 1 : (value < 0 ? -1 : 0);
     else if (k == "max_sweeps") { need(value >= 1 && value <= 1000, "max_sweeps out of range"); e.max_sweeps = (int)value; }
     else fail(MPDO_ERR_INVALID, "unknown option: " + k);
   });
@@ -1229,7 +1291,7 @@ mpdo_status mpdo_engine_profile(mpdo_engine_t eng, int enable) {
     Engine &e = eng->e;
     prof_flush(e);
     for (int c = 0; c < kProfClasses; ++c) { e.acc_ms[c] = e.acc_flops[c] = e.acc_bytes[c] = 0; e.acc_n[c] = 0; }
-    e.wide_range_hits = e.wide_exact_calls = 0;
+    e.wide_range_hits = e.wide_exact_calls = e.wide_eig_calls = 0;
     e.wide_resid_max = 0;
     e.profiling = enable != 0;
   });
@@ -1244,7 +1306,7 @@ mpdo_status mpdo_engine_profile_read(mpdo_engine_t eng, int kclass, long long *l
     prof_flush(e);
     if (kclass == 7) {   // wide-bond SVD path counters: range finder accepted / exact block Jacobi
       *launches = e.wide_range_hits;
-      *ms = 0;
+      *ms = (double)e.wide_eig_calls;
       *flops = (double)e.wide_exact_calls;
       *bytes = e.wide_resid_max;
       return;

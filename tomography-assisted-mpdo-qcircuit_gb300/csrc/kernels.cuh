@@ -119,6 +119,19 @@ void gaussian(cudaStream_t st, cx<T> *out, size_t n, uint64_t seed);
 template <typename T>
 void sumsq(cudaStream_t st, const cx<T> *x, size_t n, double *out);
 
+// Hermitian eigensolver pieces for wide-bond Gram matrices (kernels_eig.cu):
+// Householder tridiagonalisation of G (n x n, column-major) on one
+// thread-block cluster (T = Q^H G Q; d, e real; reflectors of Q as an
+// (n-1) x (n-1) column-major block with their tau), and the top kr eigenpairs
+// of the tridiagonal by bisection + inverse iteration (Z: n x kr row-major;
+// *tail = trace minus their sum).  hetrd_cluster returns the launch status
+// (a cluster that cannot be placed reports an error and launches nothing).
+template <typename T> bool hetrd_cluster_fits(int n);
+template <typename T>
+cudaError_t hetrd_cluster(cudaStream_t st, int n, const cx<T> *G, T *d, T *e, cx<T> *vref, cx<T> *tau);
+template <typename T>
+void tridiag_top(cudaStream_t st, int n, const T *d, const T *e, int kr, T *lam, cx<T> *Z, T *work, T *tail);
+
 // Message returned by mpdo_last_error() on the calling thread.
 void set_last_error(const std::string &msg);
 

@@ -30,6 +30,68 @@ template <typename T> struct Eps;
 template <> struct Eps<float> { static constexpr float v = FLT_EPSILON; static constexpr float tiny = 1e-30f; };
 template <> struct Eps<double> { static constexpr double v = DBL_EPSILON; static constexpr double tiny = 1e-290; };
 
+// One Hestenes rotation of the column pair (xp, xq) (m entries each) by one
+// warp, given their squared norms.  Returns false when the pair is already
+// orthogonal to tolerance (or at the rounding floor); otherwise rotates and
+// gives t and |g| for the norm update (alpha' = alpha - t|g|,
+// beta' = beta + t|g|) and the rotation (cs, sec, cec) for accumulating W.
+// With m <= 32 * RMAX the columns stay in registers between the inner
+// product and the rotation (one shared-memory read of each entry).
+template <typename T, int RMAX>
+__device__ __forceinline__ bool hestenes_pair(cx<T> *xp, cx<T> *xq, int m, int lane, T al, T be, T tol,
+                                              T floor_abs, T &t, T &g, T &cs, T &sn, cx<T> &sec, cx<T> &cec) {
+  const bool cached = m <= 32 * RMAX;
+  cx<T> up[RMAX], vq[RMAX];
+  cx<T> ga = czero<T>();
+  if (cached) {
+#pragma unroll
+    for (int r = 0; r < RMAX; ++r) {
+      const int i = lane + 32 * r;
+      if (i < m) {
+        up[r] = xp[i];
+        vq[r] = xq[i];
+        cfmac<T>(ga, up[r], vq[r]);
+      }
+    }
+  } else {
+    for (int i = lane; i < m; i += 32) cfmac<T>(ga, xp[i], xq[i]);
+  }
+  ga.x = wsum(ga.x); ga.y = wsum(ga.y);
+  g = sqrt(cabs2<T>(ga));
+  if (!(g > tol * sqrt(al * be)) || al <= floor_abs || be <= floor_abs || al <= Eps<T>::tiny ||
+      be <= Eps<T>::tiny || g <= Eps<T>::tiny)
+    return false;
+  const T zeta = (be - al) / (T(2) * g);
+  t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+  cs = T(1) / sqrt(T(1) + t * t);
+  sn = cs * t;
+  // e = gamma/|gamma|; x_p' = c x_p - s conj(e) x_q ; x_q' = s x_p + c conj(e) x_q
+  const cx<T> ec = cmk<T>(ga.x / g, -ga.y / g);
+  sec = cscale<T>(ec, sn);
+  cec = cscale<T>(ec, cs);
+  if (cached) {
+#pragma unroll
+    for (int r = 0; r < RMAX; ++r) {
+      const int i = lane + 32 * r;
+      if (i < m) {
+        const cx<T> u = up[r], v = vq[r];
+        const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
+        xp[i] = cmk<T>(cs * u.x - ev_s.x, cs * u.y - ev_s.y);
+        xq[i] = cmk<T>(sn * u.x + ev_c.x, sn * u.y + ev_c.y);
+      }
+    }
+  } else {
+    __syncwarp();
+    for (int i = lane; i < m; i += 32) {
+      const cx<T> u = xp[i], v = xq[i];
+      const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
+      xp[i] = cmk<T>(cs * u.x - ev_s.x, cs * u.y - ev_s.y);
+      xq[i] = cmk<T>(sn * u.x + ev_c.x, sn * u.y + ev_c.y);
+    }
+  }
+  return true;
+}
+
 template <typename T, bool SMEM>
 __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *uout, T *sigma, cx<T> *wout,
                                                cx<T> *xws, cx<T> *wws, int max_sweeps, T tol, int *status) {
@@ -93,32 +155,13 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
         const int pc = min(a, c), qc = max(a, c);
         cx<T> *xp = X + (int64_t)pc * m, *xq = X + (int64_t)qc * m;
         // squared norms carried from the sweep start through the rotations
-        // (alpha' = alpha - t|g|, beta' = beta + t|g|): one reduction per pair
         const T al = nrm[pc], be = nrm[qc];
-        cx<T> ga = czero<T>();
-        for (int i = lane; i < m; i += 32) cfmac<T>(ga, xp[i], xq[i]);
-        ga.x = wsum(ga.x); ga.y = wsum(ga.y);
-        const T g = sqrt(cabs2<T>(ga));
-        if (!(g > tol * sqrt(al * be)) || al <= floor_abs || be <= floor_abs || al <= Eps<T>::tiny ||
-            be <= Eps<T>::tiny || g <= Eps<T>::tiny)
-          continue;
-        const T zeta = (be - al) / (T(2) * g);
-        const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-        const T cs = T(1) / sqrt(T(1) + t * t);
-        const T sn = cs * t;
-        // e = gamma/|gamma|; x_p' = c x_p - s conj(e) x_q ; x_q' = s x_p + c conj(e) x_q
-        const cx<T> ec = cmk<T>(ga.x / g, -ga.y / g);
-        const cx<T> sec = cscale<T>(ec, sn), cec = cscale<T>(ec, cs);
-        __syncwarp();
+        T t, g, cs, sn;
+        cx<T> sec, cec;
+        if (!hestenes_pair<T, sizeof(T) == 4 ? 4 : 2>(xp, xq, m, lane, al, be, tol, floor_abs, t, g, cs, sn, sec, cec)) continue;
         if (lane == 0) {
           nrm[pc] = fmax(al - t * g, T(0));
           nrm[qc] = be + t * g;
-        }
-        for (int i = lane; i < m; i += 32) {
-          const cx<T> u = xp[i], v = xq[i];
-          const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
-          xp[i] = cmk<T>(cs * u.x - ev_s.x, cs * u.y - ev_s.y);
-          xq[i] = cmk<T>(sn * u.x + ev_c.x, sn * u.y + ev_c.y);
         }
         if (wantW) {
           cx<T> *wp = W + (int64_t)pc * n, *wq = W + (int64_t)qc * n;
@@ -225,28 +268,12 @@ __global__ void __launch_bounds__(512) k_bjacobi(int m, int n, int bs, int nblk,
   // reduction (its inner product) instead of three
   __shared__ T nrm2[64];
   auto rotate_pair = [&](int pc, int qc) -> bool {
-    cx<T> *xp = S + (int64_t)pc * m, *xq = S + (int64_t)qc * m;
-    cx<T> ga = czero<T>();
-    for (int i = lane; i < m; i += 32) cfmac<T>(ga, xp[i], xq[i]);
-    ga.x = wsum(ga.x); ga.y = wsum(ga.y);
     const T al = nrm2[pc], be = nrm2[qc];
-    const T g = sqrt(cabs2<T>(ga));
-    if (!(g > tol * sqrt(al * be)) || al <= floor_abs || be <= floor_abs || al <= Eps<T>::tiny ||
-        be <= Eps<T>::tiny || g <= Eps<T>::tiny)
+    T t, g, cs, sn;
+    cx<T> sec, cec;
+    if (!hestenes_pair<T, sizeof(T) == 4 ? 8 : 4>(S + (int64_t)pc * m, S + (int64_t)qc * m, m, lane, al, be, tol, floor_abs, t, g, cs,
+                              sn, sec, cec))
       return false;
-    const T zeta = (be - al) / (T(2) * g);
-    const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-    const T cs = T(1) / sqrt(T(1) + t * t);
-    const T sn = cs * t;
-    const cx<T> ec = cmk<T>(ga.x / g, -ga.y / g);
-    const cx<T> sec = cscale<T>(ec, sn), cec = cscale<T>(ec, cs);
-    __syncwarp();
-    for (int i = lane; i < m; i += 32) {
-      const cx<T> u = xp[i], v = xq[i];
-      const cx<T> ev_s = cmul<T>(sec, v), ev_c = cmul<T>(cec, v);
-      xp[i] = cmk<T>(cs * u.x - ev_s.x, cs * u.y - ev_s.y);
-      xq[i] = cmk<T>(sn * u.x + ev_c.x, sn * u.y + ev_c.y);
-    }
     if (lane == 0) {
       nrm2[pc] = fmax(al - t * g, T(0));
       nrm2[qc] = be + t * g;

@@ -209,6 +209,17 @@ __global__ void __launch_bounds__(QR_NT) k_qr_apply(int m, int n, int mc, const 
                                                     const cx<T> *bin, int64_t ldb, int nq, cx<T> *qout,
                                                     int64_t ldq) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // blockIdx.y selects a group of gridDim.y-way split columns of B (groups
+  // sized so that each fits shared memory)
+  int q0 = 0;
+  {
+    const int per = (nq + gridDim.y - 1) / gridDim.y;
+    q0 = blockIdx.y * per;
+    if (bin) bin += q0;
+    qout += q0;
+    nq = max(0, min(per, nq - q0));
+    if (nq == 0) return;
+  }
   const int c = blockIdx.x;
   const int r0 = c * mc;
   const int rows = min(mc, m - r0);
@@ -229,7 +240,7 @@ __global__ void __launch_bounds__(QR_NT) k_qr_apply(int m, int n, int mc, const 
     cx<T> v = czero<T>();
     if (i < kc) {
       if (bin) v = bin[(int64_t)(c * n + i) * ldb + q];
-      else v = (i == q) ? cmk<T>(T(1), T(0)) : czero<T>();
+      else v = (i == q + q0) ? cmk<T>(T(1), T(0)) : czero<T>();
     }
     B(i, q) = v;
   }
@@ -305,10 +316,16 @@ void qr_factor_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const 
 template <typename T>
 void qr_apply_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const cx<T> *vws, const cx<T> *tau,
                      const cx<T> *bin, int64_t ldb, int nq, cx<T> *qout, int64_t ldq) {
-  const size_t bytes = ((size_t)2 * mc + (size_t)mc * nq) * sizeof(cx<T>);
-  if (bytes <= SMEM_CAP) {
+  // columns of B are split into groups that fit shared memory next to the
+  // two reflector buffers, one CTA per (chunk, group)
+  const size_t esz = sizeof(cx<T>);
+  const int64_t fit = ((int64_t)(SMEM_CAP / esz) - 2 * (int64_t)mc) / std::max(mc, 1);
+  const int groups = fit >= 1 ? (int)((nq + fit - 1) / fit) : 0;
+  if (groups >= 1 && groups <= 64) {
+    const int per = (nq + groups - 1) / groups;
+    const size_t bytes = ((size_t)2 * mc + (size_t)mc * per) * esz;
     smem_optin(k_qr_apply<T, true>);
-    k_qr_apply<T, true><<<nchunks, QR_NT, bytes, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
+    k_qr_apply<T, true><<<dim3(nchunks, groups), QR_NT, bytes, st>>>(m, n, mc, vws, tau, bin, ldb, nq, qout, ldq);
   } else {
     const size_t vb = (size_t)2 * mc * sizeof(cx<T>);
     smem_optin(k_qr_apply<T, false>);

@@ -78,7 +78,8 @@ class Engine:
                                          m, n, int(keep), _dptr(_cplx(y)), _dptr(lo), _dptr(ro)))
         return lo.view(np.complex128).reshape(m, keep), ro.view(np.complex128).reshape(keep, n)
 
-    KERNEL_CLASSES = ('gemm', 'qr_factor', 'qr_apply', 'jacobi', 'kraus1q', 'mix2q', 'other', None, 'bjacobi')
+    KERNEL_CLASSES = ('gemm', 'qr_factor', 'qr_apply', 'jacobi', 'kraus1q', 'mix2q', 'other', None, 'bjacobi',
+                      None, None, None, None, 'hetrd')
     PHASES = ('qr_sweep', 'svd_sweep', 'kappa_pass', 'wide_svd')
 
     def profile(self, enable: bool) -> None:
@@ -98,7 +99,8 @@ class Engine:
             out[name] = dict(launches=int(n.value), ms=ms.value, flops=fl.value, bytes=by.value)
         n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
         check(self._lib.mpdo_engine_profile_read(self.handle, 7, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
-        out['wide_bonds'] = dict(range_finder=int(n.value), exact=int(fl.value), max_residual=by.value)
+        out['wide_bonds'] = dict(range_finder=int(n.value), exact=int(fl.value), max_residual=by.value,
+                                 tridiagonal=int(ms.value))
         phases = {}
         for i, name in enumerate(self.PHASES, start=9):
             n, ms, fl, by = C.c_longlong(), C.c_double(), C.c_double(), C.c_double()
