@@ -62,8 +62,8 @@ def parse():
     ap.add_argument('--dtype', default='complex64')
     ap.add_argument('--cpu-budget', type=float, default=20.0, help='seconds of CPU work for the baseline sample')
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--batch', type=int, default=16, help='independent circuits per step (seeds)')
-    ap.add_argument('--workers', type=int, default=16, help='worker engines of the batch runner')
+    ap.add_argument('--batch', type=int, default=24, help='independent circuits per step (seeds)')
+    ap.add_argument('--workers', type=int, default=24, help='worker engines of the batch runner')
     ap.add_argument('--plain-steps', type=int, default=1, help='timed single-circuit runs (reported as plain)')
     ap.add_argument('--plain-warmup', type=int, default=1)
     return ap.parse_args()
