@@ -75,6 +75,8 @@ mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
  *                outside its span is at rounding level, so the triplets are
  *                those of an exact SVD): 1 always, 0 never (Gram +
  *                block-Jacobi path only), -1 (default) complex128 only.
+ *   "wide_range_tol" acceptance factor of the range finder: the residual must
+ *                be <= factor * eps * sqrt(p) * |Y|_F (default 8, rounding level).
  *   "wide_eig"   the exact wide-bond path diagonalises the Gram matrix by
  *                Householder tridiagonalisation on a thread-block cluster +
  *                bisection / inverse iteration (1), or by block Jacobi (0);

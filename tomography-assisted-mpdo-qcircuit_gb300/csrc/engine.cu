@@ -59,6 +59,7 @@ struct Engine {
   long long wide_eig_calls = 0;
   long long wide_range_hits = 0, wide_exact_calls = 0;
   double wide_resid_max = 0;        // largest accepted |Y - Q Q^H Y|_F / |Y|_F
+  double wide_range_tol = 8.0;      // acceptance: residual <= tol * eps * sqrt(p) * |Y|_F
   int max_sweeps = 60;
   int first_status = 0;
   // per-kernel-class profiling (CUDA events around each launch)
@@ -539,7 +540,7 @@ static bool left_svd_wide_range(Engine &e, const cx<T> *Y, int Mr, int Nc, int w
   if (p >= Mr) return false;
   const T eps = sizeof(T) == 4 ? T(1.1920929e-7) : T(2.220446049250313e-16);
   // rounding level of the residual itself: |fl(Y - Q (Q^H Y))|_F ~ eps sqrt(p) |Y|_F
-  const double tol = 8.0 * eps * std::sqrt((double)p);
+  const double tol = e.wide_range_tol * eps * std::sqrt((double)p);
   DBuf<double> nrm(e, 2);
   sumsq<T>(e.stream, Y, (size_t)Mr * Nc, nrm.p);
   DBuf<cx<T>> Z(e, (size_t)Mr * p), Q(e, (size_t)Mr * p), Rq(e, (size_t)p * p), B(e, (size_t)p * Nc),
@@ -1280,6 +1281,10 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
     if (k == "fuse_2q") e.fuse_2q = value != 0;
     else if (k == "wide_range") e.wide_range = value > 0 ? 1 : (value < 0 ? -1 : 0);
     else if (k == "wide_eig") e.wide_eig = value > 0 ? 1 : (value < 0 ? -1 : 0);
+    else if (k == "wide_range_tol") {
+      need(value > 0, "wide_range_tol must be positive");
+      e.wide_range_tol = value;
+    }
     else if (k == "max_sweeps") { need(value >= 1 && value <= 1000, "max_sweeps out of range"); e.max_sweeps = (int)value; }
     else fail(MPDO_ERR_INVALID, "unknown option: " + k);
   });
