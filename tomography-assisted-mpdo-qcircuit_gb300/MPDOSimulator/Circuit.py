@@ -72,11 +72,16 @@ class TensorCircuit(QuantumCircuit):
     def _np(t) -> np.ndarray:
         return t.detach().to('cpu', torch.complex128).numpy()
 
+    @staticmethod
+    def _gate_np(gate: QuantumGate) -> np.ndarray:
+        f = getattr(gate, 'numpy_tensor', None)
+        return f() if f is not None else gate.tensor.detach().to('cpu', torch.complex128).numpy()
+
     def _noisy_1q(self, gate: QuantumGate) -> np.ndarray:
         """Circuit.py:141-155 (composite cached per name for fixed gates)."""
-        g = gate.tensor
+        g = self._gate_np(gate)
         if not ((self.idealNoise or self.unified) and not gate.ideal):
-            return self._np(g)
+            return g
         key = None if (gate.variational or gate.name == 'ArbSingleGate') else gate.name
         if key is not None and key in self.noiseTensorDict:
             return self.noiseTensorDict[key]
@@ -87,7 +92,7 @@ class TensorCircuit(QuantumCircuit):
             self._noise_pre = np.einsum('nlm,ljk->njmk', self._np(self.Noise.decayTensor),
                                         self._np(self.Noise.dephasingTensor))
             self._noise_pre_key = pre_key
-        t = np.einsum('njmk,ji->nimk', self._noise_pre, self._np(g)).reshape(2, 2, -1)
+        t = np.einsum('njmk,ji->nimk', self._noise_pre, g).reshape(2, 2, -1)
         if key is not None:
             self.noiseTensorDict[key] = t
         return t

@@ -185,3 +185,16 @@ class _Param(QuantumGate):
     def tensor(self):
         t = self._build()
         return t if self._SINGLE else t.reshape(2, 2, 2, 2)
+
+    def numpy_tensor(self):
+        """The gate as a complex128 numpy array, for the engine (which takes
+        host Kraus tensors).  Gates that define ``_build_np`` evaluate it on
+        plain floats when no parameter needs a gradient (the angles rounded to
+        the circuit's real precision, as ``_check_Para_Tensor`` stores them);
+        otherwise the autograd-capable ``tensor`` is converted."""
+        params = self.para if isinstance(self.para, (list, tuple)) else [self.para]
+        if hasattr(self, '_build_np') and all(isinstance(q, Tensor) and not q.requires_grad and not q.is_complex()
+                                              for q in params):
+            t = self._build_np(*[float(q) for q in params])
+            return t if self._SINGLE else t.reshape(2, 2, 2, 2)
+        return self.tensor.detach().to('cpu', torch.complex128).numpy()

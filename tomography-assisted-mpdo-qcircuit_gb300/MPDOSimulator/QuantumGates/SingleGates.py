@@ -1,8 +1,10 @@
 """Single-qubit gates (reference: QuantumGates/SingleGates.py)."""
+import cmath
 import math
 from typing import Optional, Union
 from warnings import warn
 
+import numpy as np
 import torch
 from torch import Tensor
 
@@ -56,6 +58,12 @@ class U3Gate(_Param):                                          # SingleGates.py:
         lm, pm = _cexp(self.lam), _cexp(self.phi)
         c, s = torch.cos(self.theta / 2), torch.sin(self.theta / 2)
         return self._mat([[c, -lm * s], [pm * s, lm * pm * c]])
+
+    @staticmethod
+    def _build_np(theta, phi, lam):
+        c, s = math.cos(theta / 2), math.sin(theta / 2)
+        el, ep = cmath.exp(1j * lam), cmath.exp(1j * phi)
+        return np.array([[c, -el * s], [ep * s, el * ep * c]], dtype=np.complex128)
 
 
 class ArbSingleGate(QuantumGate):                              # SingleGates.py:204-237

@@ -1,6 +1,9 @@
 """X-family gates (reference: QuantumGates/XGates.py)."""
+import cmath
+import math
 from typing import Optional
 
+import numpy as np
 import torch
 
 from .AbstractGate import _Fixed, _Param
@@ -21,6 +24,11 @@ class RXGate(_Param):                                          # XGates.py:48-85
     def _build(self):
         c, s = torch.cos(self.theta / 2), torch.sin(self.theta / 2)
         return self._mat([[c, -1j * s], [-1j * s, c]])
+
+    @staticmethod
+    def _build_np(theta):
+        c, s = math.cos(theta / 2), math.sin(theta / 2)
+        return np.array([[c, -1j * s], [-1j * s, c]], dtype=np.complex128)
 
 
 class CXGate(_Fixed):                                          # XGates.py:88-120

@@ -1,6 +1,9 @@
 """Y-family gates (reference: QuantumGates/YGates.py)."""
+import cmath
+import math
 from typing import Optional
 
+import numpy as np
 import torch
 
 from .AbstractGate import _Fixed, _Param
@@ -21,6 +24,11 @@ class RYGate(_Param):                                          # YGates.py:48-85
     def _build(self):
         c, s = torch.cos(self.theta / 2), torch.sin(self.theta / 2)
         return self._mat([[c, -s], [s, c]])
+
+    @staticmethod
+    def _build_np(theta):
+        c, s = math.cos(theta / 2), math.sin(theta / 2)
+        return np.array([[c, -s], [s, c]], dtype=np.complex128)
 
 
 class CYGate(_Fixed):                                          # YGates.py:88-121

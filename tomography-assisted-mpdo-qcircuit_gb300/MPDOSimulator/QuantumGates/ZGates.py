@@ -1,6 +1,9 @@
 """Z-family gates (reference: QuantumGates/ZGates.py)."""
+import cmath
+import math
 from typing import Optional
 
+import numpy as np
 import torch
 
 from .AbstractGate import _Fixed, _Param, _cexp
@@ -20,6 +23,10 @@ class RZGate(_Param):                                          # ZGates.py:48-84
 
     def _build(self):
         return self._mat([[_cexp(-self.theta / 2), 0], [0, _cexp(self.theta / 2)]])
+
+    @staticmethod
+    def _build_np(theta):
+        return np.array([[cmath.exp(-0.5j * theta), 0], [0, cmath.exp(0.5j * theta)]], dtype=np.complex128)
 
 
 class CZGate(_Fixed):                                          # ZGates.py:87-119
