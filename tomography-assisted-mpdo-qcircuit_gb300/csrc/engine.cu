@@ -357,6 +357,47 @@ static void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
 // the rotations accumulated: R W = U diag(sigma).  W (n x n, column-major,
 // columns sorted by sigma descending) is unitary to rounding whatever the
 // rank; sigma has n entries (zeros beyond the rank).
+// R factors of a batch of equally shaped m x n matrices (input b at in.bs*b):
+// R (batch x k x n, row-major, k = min(m, n)), by the same TSQR levels as qr().
+template <typename T>
+static void qr_r_batched(Engine &e, int batch, int m, int n, const View<T> &in, cx<T> *R) {
+  const size_t esz = sizeof(cx<T>);
+  const size_t cap = 200 * 1024;
+  DBuf<cx<T>> v, tau, rs, rs_prev;
+  View<T> cur = in;
+  int curm = m, last_nch = 1;
+  while (true) {
+    int mc;
+    if ((size_t)curm * (n + 2) * esz <= cap) mc = curm;
+    else {
+      size_t mcs = cap / ((size_t)(n + 2) * esz);
+      mcs = mcs / 32 * 32;
+      mc = (mcs > (size_t)n) ? (int)std::min<size_t>(mcs, (size_t)curm) : curm;
+    }
+    const int nch = (curm + mc - 1) / mc;
+    v = DBuf<cx<T>>(e, (size_t)batch * nch * mc * n);
+    tau = DBuf<cx<T>>(e, (size_t)batch * nch * n);
+    rs = DBuf<cx<T>>(e, (size_t)batch * nch * n * n);
+    {
+      const double mm = (double)std::min(mc, curm), nn = n, kk = std::min(mm, nn);
+      const double fl = batch * nch * 4.0 * (2.0 * mm * nn * kk - (mm + nn) * kk * kk + 2.0 / 3.0 * kk * kk * kk);
+      const double by = (double)esz * batch * ((double)curm * n + (double)nch * n * n);
+      prof(e, K_QR_FACTOR, fl, by,
+           [&] { qr_factor_chunks<T>(e.stream, curm, n, mc, nch, cur, v.p, tau.p, rs.p, batch); });
+    }
+    last_nch = nch;
+    if (nch == 1) break;
+    rs_prev = std::move(rs);
+    cur = View<T>{rs_prev.p, (int64_t)nch * n * n, 1, n, 0, 1, 0};
+    curm = (nch - 1) * n + std::min(n, curm - (nch - 1) * mc);
+  }
+  (void)last_nch;
+  const int k = std::min(m, n);
+  if (std::min(curm, n) != k) fail(MPDO_ERR_BAD_SHAPE, "internal TSQR rank mismatch");
+  MPDO_CUDA_CHECK(cudaMemcpy2DAsync(R, (size_t)k * n * esz, rs.p, (size_t)n * n * esz, (size_t)k * n * esz, batch,
+                                    cudaMemcpyDeviceToDevice, e.stream));
+}
+
 template <typename T>
 static void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W, DBuf<T> &sigma) {
   const int k = std::min(m, n);
@@ -854,36 +895,69 @@ template <typename T> static void kappa_pass(mpdo_chain_s *ch, int kappa, double
   Engine &e = ch->eng->e;
   Phase ph(e, P_KAPPA);
   if (kappa <= 0 && max_err < 0) return;
+  // sites that need the pass, grouped by shape: without an error rule the
+  // kept count is known on the host, so each group runs as one batch
+  std::vector<int> todo;
   for (int i = 0; i < ch->n; ++i) {
     const Site s = ch->s[i];
     if (s.a == 1 || (kappa > 0 && s.a <= kappa)) continue;
-    const int rows = s.l * 2 * s.r, a = s.a;
-    DBuf<cx<T>> Am(e, (size_t)rows * a);
-    {
-      const int64_t d[4] = {s.l, 2, s.r, a};
-      const int64_t st[4] = {(int64_t)2 * a * s.r, (int64_t)a * s.r, 1, s.r};
-      copy4d<T>(e.stream, Am.p, site_ptr<T>(ch, i), d, st, 0);
-    }
-    DBuf<cx<T>> V;
-    DBuf<T> sg;
-    right_svd<T>(e, rows, a, RM<T>(Am.p, a), V, sg);
+    todo.push_back(i);
+  }
+  std::vector<bool> done(ch->n, false);
+  for (size_t t = 0; t < todo.size(); ++t) {
+    const int i0 = todo[t];
+    if (done[i0]) continue;
+    const Site s0 = ch->s[i0];
+    std::vector<int> grp{i0};
+    if (max_err < 0)
+      for (size_t u = t + 1; u < todo.size(); ++u) {
+        const Site su = ch->s[todo[u]];
+        if (!done[todo[u]] && su.l == s0.l && su.r == s0.r && su.a == s0.a) grp.push_back(todo[u]);
+      }
+    for (int i : grp) done[i] = true;
+    const int B = (int)grp.size();
+    const int rows = s0.l * 2 * s0.r, a = s0.a;
     const int nsv = std::min(rows, a);
+    // (l, s, r) x a per site, consecutive
+    DBuf<cx<T>> Am(e, (size_t)B * rows * a);
+    for (int b = 0; b < B; ++b) {
+      const int64_t d[4] = {s0.l, 2, s0.r, a};
+      const int64_t st[4] = {(int64_t)2 * a * s0.r, (int64_t)a * s0.r, 1, s0.r};
+      copy4d<T>(e.stream, Am.p + (size_t)b * rows * a, site_ptr<T>(ch, grp[b]), d, st, 0);
+    }
+    // right singular vectors: R of each (QR), then one-sided Jacobi with V
+    const int k = nsv;
+    DBuf<cx<T>> R(e, (size_t)B * k * a), V(e, (size_t)B * a * a), Ub(e, (size_t)B * k * a),
+        xws(e, (size_t)B * k * a), wws(e, (size_t)B * a * a);
+    DBuf<T> sg(e, (size_t)B * a);
+    qr_r_batched<T>(e, B, rows, a, View<T>{Am.p, (int64_t)rows * a, 1, a, 0, 1, 0}, R.p);
+    {
+      const double mm = std::max(k, a), nn = std::min(k, a);
+      const double fl = B * 4.0 * (4.0 * mm * nn * nn + 22.0 * nn * nn * nn);
+      int *slot = status_slot(e, B);
+      prof(e, K_JACOBI, fl, (double)sizeof(cx<T>) * B * ((double)k * a * 2 + (double)a * a), [&] {
+        jacobi_svd<T>(e.stream, B, k, a, View<T>{R.p, (int64_t)k * a, 1, a, 0, 1, 0}, Ub.p, sg.p, V.p, xws.p,
+                      wws.p, e.max_sweeps, slot);
+      });
+    }
     int keep = kappa > 0 ? std::min(kappa, nsv) : nsv;
-    if (max_err >= 0) {
+    if (max_err >= 0) {            // (B == 1 here)
       std::vector<T> sv(nsv);
       MPDO_CUDA_CHECK(cudaMemcpyAsync(sv.data(), sg.p, nsv * sizeof(T), cudaMemcpyDeviceToHost, e.stream));
       MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
       keep = error_rule_keep<T>(sv, nsv, keep, max_err, true);
     }
-    DBuf<cx<T>> NM(e, (size_t)rows * keep);
-    gemm<T>(e, rows, keep, a, RM<T>(Am.p, a), CM<T>(V.p, a), NM.p, keep);
-    DBuf<cx<T>> NS(e, (size_t)rows * keep);
-    {
-      const int64_t d[4] = {s.l, 2, keep, s.r};
-      const int64_t st[4] = {(int64_t)2 * s.r * keep, (int64_t)s.r * keep, 1, keep};
-      copy4d<T>(e.stream, NS.p, NM.p, d, st, 0);
+    // site := U S = A V[:, :keep]
+    DBuf<cx<T>> NM(e, (size_t)B * rows * keep);
+    gemm<T>(e, rows, keep, a, View<T>{Am.p, (int64_t)rows * a, 1, a, 0, 1, 0},
+            View<T>{V.p, (int64_t)a * a, 1, 1, 0, a, 0}, NM.p, keep, B, (int64_t)rows * keep);
+    for (int b = 0; b < B; ++b) {
+      DBuf<cx<T>> NS(e, (size_t)rows * keep);
+      const int64_t d[4] = {s0.l, 2, keep, s0.r};
+      const int64_t st[4] = {(int64_t)2 * s0.r * keep, (int64_t)s0.r * keep, 1, keep};
+      copy4d<T>(e.stream, NS.p, NM.p + (size_t)b * rows * keep, d, st, 0);
+      set_site<T>(ch, grp[b], NS.release(), s0.l, keep, s0.r);
     }
-    set_site<T>(ch, i, NS.release(), s.l, keep, s.r);
   }
 }
 

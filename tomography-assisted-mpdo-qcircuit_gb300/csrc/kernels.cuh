@@ -23,9 +23,11 @@ void cgemm(cudaStream_t st, int M, int N, int K, int batch, cx<T> alpha, const V
 // vectors and tau are kept in `vws` (mc x n column-major per chunk) and `tau`
 // (n per chunk); R_c (kc x n, kc = min(rows_c, n)) is written row-major into
 // `rstack` at row offset c*n (rows kc..n-1 of the slot are zero-filled).
+// batch > 1 factors that many matrices (input b at in.bs * b), each with its
+// own consecutive nchunks slots of vws / tau / rstack.
 template <typename T>
 void qr_factor_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const View<T> &in, cx<T> *vws,
-                      cx<T> *tau, cx<T> *rstack);
+                      cx<T> *tau, cx<T> *rstack, int batch = 1);
 
 // Q_c = H_c(0) ... H_c(kc-1) [B_c; 0] for every chunk, where B_c is the
 // kc x nq block of `bin` (row-major, leading dimension ldb) starting at row

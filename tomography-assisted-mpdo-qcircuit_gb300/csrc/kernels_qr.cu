@@ -86,6 +86,13 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ cx<T> hh[2];  // tau, scale
   __shared__ T cn[4];      // scaled norm parts of the next column, by parity
+  // blockIdx.y: matrix of a batch (input at batch stride in.bs; each
+  // matrix's reflectors, tau and R stack in consecutive slots)
+  const int bb = blockIdx.y;
+  const int nchunks = gridDim.x;
+  vws += (int64_t)bb * nchunks * mc * n;
+  tau_out += (int64_t)bb * nchunks * n;
+  rstack += (int64_t)bb * nchunks * n * n;
   const int c = blockIdx.x;
   const int r0 = c * mc;
   const int rows = min(mc, m - r0);
@@ -97,7 +104,7 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
 
   for (int64_t idx = tid; idx < (int64_t)rows * n; idx += blockDim.x) {
     const int i = (int)(idx % rows), j = (int)(idx / rows);
-    W[j * ld + i] = view_ld(in, 0, r0 + i, j);
+    W[j * ld + i] = view_ld(in, bb, r0 + i, j);
   }
   __syncthreads();
 
@@ -302,13 +309,14 @@ __global__ void __launch_bounds__(QR_NT) k_qr_apply(int m, int n, int mc, const 
 
 template <typename T>
 void qr_factor_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const View<T> &in, cx<T> *vws,
-                      cx<T> *tau, cx<T> *rstack) {
+                      cx<T> *tau, cx<T> *rstack, int batch) {
   const size_t bytes = (size_t)mc * n * sizeof(cx<T>);
+  const dim3 grid(nchunks, std::max(batch, 1));
   if (bytes <= SMEM_CAP) {
     smem_optin(k_qr_factor<T, true>);
-    k_qr_factor<T, true><<<nchunks, QR_NT, bytes, st>>>(m, n, mc, in, vws, tau, rstack);
+    k_qr_factor<T, true><<<grid, QR_NT, bytes, st>>>(m, n, mc, in, vws, tau, rstack);
   } else {
-    k_qr_factor<T, false><<<nchunks, QR_NT, 0, st>>>(m, n, mc, in, vws, tau, rstack);
+    k_qr_factor<T, false><<<grid, QR_NT, 0, st>>>(m, n, mc, in, vws, tau, rstack);
   }
   count_launch();
 }
@@ -335,9 +343,9 @@ void qr_apply_chunks(cudaStream_t st, int m, int n, int mc, int nchunks, const c
 }
 
 template void qr_factor_chunks<float>(cudaStream_t, int, int, int, int, const View<float> &, cx<float> *,
-                                      cx<float> *, cx<float> *);
+                                      cx<float> *, cx<float> *, int);
 template void qr_factor_chunks<double>(cudaStream_t, int, int, int, int, const View<double> &, cx<double> *,
-                                       cx<double> *, cx<double> *);
+                                       cx<double> *, cx<double> *, int);
 template void qr_apply_chunks<float>(cudaStream_t, int, int, int, int, const cx<float> *, const cx<float> *,
                                      const cx<float> *, int64_t, int, cx<float> *, int64_t);
 template void qr_apply_chunks<double>(cudaStream_t, int, int, int, int, const cx<double> *,
