@@ -81,6 +81,11 @@ def dist_init(args):
     return rank, ws, local
 
 
+def replica_seeds(rank, per_rank):
+    """Circuit seeds of one rank: every rank evolves its own, disjoint set."""
+    return [rank * per_rank + k for k in range(per_rank)]
+
+
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -308,7 +313,7 @@ def gpu_arm(args):
         os.path.join(ROOT, 'MEASURED_PEAKS.json')) else {}
     cdt = torch.complex64 if args.dtype == 'complex64' else torch.complex128
     B = max(1, args.batch)
-    seeds = [rank * B + k for k in range(B)]
+    seeds = replica_seeds(rank, B)
     works = [workload(args, seed=s) for s in seeds]
     w = works[0]
     gates_per_circuit = w.gates

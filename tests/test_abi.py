@@ -52,3 +52,29 @@ def test_no_device_fails_loudly(lib):
     from mpdo_gb300._lib import MPDOError
     with pytest.raises(MPDOError, match='no CUDA device'):
         Engine(0)
+
+
+def test_status_codes_map_to_reference_exceptions(lib):
+    # the reference raises torch.linalg.LinAlgError when its SVD fails
+    # (Circuit.py:127-136) and ValueError on bad arguments
+    import torch
+    from mpdo_gb300 import _lib
+    cases = [(_lib.MPDO_ERR_INVALID, ValueError), (_lib.MPDO_ERR_BAD_SHAPE, ValueError),
+             (_lib.MPDO_ERR_NOT_CONVERGED, torch.linalg.LinAlgError), (_lib.MPDO_ERR_NONFINITE, torch.linalg.LinAlgError),
+             (_lib.MPDO_ERR_OOM, MemoryError), (_lib.MPDO_ERR_CUDA, _lib.MPDOError),
+             (_lib.MPDO_ERR_NO_DEVICE, _lib.MPDOError)]
+    for status, exc in cases:
+        with pytest.raises(exc):
+            _lib.check(status)
+        assert lib.mpdo_status_string(status)
+    _lib.check(_lib.MPDO_OK)
+
+
+def test_batch_arguments_checked_before_any_device_work(lib):
+    import ctypes as C
+    from mpdo_gb300 import _lib
+    h = C.c_void_p()
+    assert lib.mpdo_batch_create(0, 0, C.byref(h)) == _lib.MPDO_ERR_INVALID
+    assert b'workers' in lib.mpdo_last_error()
+    assert lib.mpdo_batch_run(None, 1, None, None, None, None) == _lib.MPDO_ERR_INVALID
+    assert lib.mpdo_batch_error(None, 0) == b''

@@ -1,0 +1,65 @@
+"""bench.py's multi-process path on CPU (gloo, world size 2): the rank
+bookkeeping, barrier and max-over-ranks timing, and the reference arm, where
+rank 0 alone measures and prints while the other rank exits cleanly."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(('127.0.0.1', 0))
+        return s.getsockname()[1]
+
+
+def _launch(code_or_args, port, ws=2, timeout=600):
+    procs = []
+    for r in range(ws):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(ws), MASTER_ADDR='127.0.0.1',
+                   MASTER_PORT=str(port), CUDA_VISIBLE_DEVICES='')
+        procs.append(subprocess.Popen([sys.executable] + code_or_args, cwd=ROOT, env=env, stdout=subprocess.PIPE,
+                                      stderr=subprocess.PIPE, text=True))
+    outs = []
+    for p in procs:
+        try:
+            out, err = p.communicate(timeout=timeout)
+        except subprocess.TimeoutExpired:
+            p.kill()
+            raise
+        outs.append((p.returncode, out, err))
+    return outs
+
+
+def test_gloo_barrier_and_max_over_ranks():
+    code = ("import sys, json; sys.argv = ['bench.py', '--impl', 'reference']; import bench; "
+            "args = bench.parse(); rank, ws, local = bench.dist_init(args); "
+            "bench.barrier(ws); m = bench.allreduce_max(1.5 + rank, ws); bench.barrier(ws); "
+            "print(json.dumps({'rank': rank, 'ws': ws, 'max': m, 'seeds': bench.replica_seeds(rank, 3)}))")
+    outs = _launch(['-c', code], _free_port())
+    got = [json.loads(o[1].strip().splitlines()[-1]) for o in outs]
+    for rc, _, err in outs:
+        assert rc == 0, err[-2000:]
+    assert sorted(g['rank'] for g in got) == [0, 1]
+    assert all(g['ws'] == 2 and g['max'] == 2.5 for g in got)
+    seeds = [s for g in got for s in g['seeds']]
+    assert len(set(seeds)) == len(seeds) == 6           # replicas evolve disjoint circuits
+
+
+@pytest.mark.timeout(900)
+def test_reference_arm_rank0_only():
+    args = ['bench.py', '--impl', 'reference', '--gpus', '2', '--n', '6', '--depth', '2', '--chi', '4', '--kappa',
+            '2', '--steps', '1', '--warmup', '1', '--cpu-budget', '2', '--batch', '2']
+    outs = _launch(args, _free_port())
+    for rc, _, err in outs:
+        assert rc == 0, err[-2000:]
+    lines = [[ln for ln in o[1].splitlines() if ln.startswith('{')] for o in outs]
+    assert len(lines[0]) == 1 and lines[1] == []
+    d = json.loads(lines[0][0])
+    assert d['impl'] == 'reference' and d['value'] > 0 and d['unit'] == 'gates/s'
+    assert d['cpu_baseline']['value'] == d['value'] and d['e2e']['h2d_bytes_per_step'] == 0
