@@ -23,6 +23,7 @@
  *   mpdo_expect_ops        dmOperations.py:135-201 expect / pauli_expect
  *                          (single-site operator products)
  *   mpdo_expect_pauli_batch  many pauli_expect terms sharing one pass
+ *   mpdo_sample            Circuit.py:297-446 sample (conditional sampling)
  *
  * Layout of a site tensor in device memory: complex, row-major
  * A[l][s][a][r] (l left bond, s physical = 2, a Kraus leg I_k, r right bond).
@@ -160,6 +161,15 @@ mpdo_status mpdo_expect_ops(mpdo_chain_t ch, const int *sites, const double *ops
 /* nterms Pauli strings, paulis[t*n + q] in {0:I, 1:X, 2:Y, 3:Z}; out[t] = Re Tr(rho P_t). */
 mpdo_status mpdo_expect_pauli_batch(mpdo_chain_t ch, const int8_t *paulis, int nterms,
                                     double *out);
+
+/* Circuit.py:297-446 sample (conditional, grouped by measured prefix): L
+ * ascending qubits `order` are sampled, the others traced; bits_out is
+ * shots x L (row-major, 0/1).  pfloor is added to both conditional
+ * probabilities (GLOBAL_MINIMUM in the reference); seed drives the host
+ * binomial splits.  Right environments are built once and every group's
+ * left environment advances in one batched step per measured qubit. */
+mpdo_status mpdo_sample(mpdo_chain_t ch, const int *order, int L, int64_t shots, uint64_t seed, double pfloor,
+                        int8_t *bits_out);
 
 /* ---- Batched evolution of independent circuits ----------------------------
  * A batch runner owns `workers` host threads, each with its own engine (its

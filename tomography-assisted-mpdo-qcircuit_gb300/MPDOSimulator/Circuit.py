@@ -272,7 +272,10 @@ class TensorCircuit(QuantumCircuit):
                reduced: Optional[List[int]] = None, sample_string: bool = True, _tqdm_disable: bool = False,
                _require_sequential_sample: bool = False, _require_bool_result: bool = False,
                _require_counts: bool = True, _stateNodes4Sample=None):
-        """Circuit.py:389-446 (batch conditional sampling, 344-387)."""
+        """Circuit.py:389-446 (batch conditional sampling, 344-387): shots
+        sharing a measured prefix form one group; each group's conditional
+        probability p(1 | prefix) (GLOBAL_MINIMUM added to both outcomes)
+        splits it binomially."""
         shots = shots or 1024
         reduced = reduced or []
         order = [q for q in range(self.qnumber) if q not in reduced]
@@ -287,29 +290,13 @@ class TensorCircuit(QuantumCircuit):
                 g = self._np(M(dtype=self.dtype, device='cpu').tensor)
                 for q in idx:
                     chain.apply_1q(q, g)
-        seq = torch.zeros((shots, L), dtype=torch.bool if _require_bool_result else torch.int)
-        one = True if _require_bool_result else 1
-        groups = [self.Group(history=[], start=0, length=shots)]
-        for pos in range(L):
-            new = []
-            for grp in groups:
-                if grp.length == 0:
-                    continue
-                p1 = self._conditional_prb(chain, order, grp.history)
-                if p1 < GLOBAL_MINIMUM:
-                    k1 = 0
-                elif p1 > 1 - GLOBAL_MINIMUM:
-                    k1 = grp.length
-                else:
-                    k1 = int(torch.bernoulli(torch.full((grp.length,), p1)).sum())
-                k0 = grp.length - k1
-                seq[grp.start: grp.start + k1, pos] = one
-                if pos < L - 1:
-                    if k1 > 0:
-                        new.append(self.Group(grp.history + [1], grp.start, k1))
-                    if k0 > 0:
-                        new.append(self.Group(grp.history + [0], grp.start + k1, k0))
-            groups = new
+        # conditional sampling on the GPU (right environments cached, all
+        # groups of a prefix advanced together); the binomial splits draw
+        # from a seed taken from torch's generator, so torch.manual_seed
+        # makes runs reproducible
+        seed = int(torch.randint(0, 2 ** 62, (1,)).item())
+        raw = chain.sample(order, shots, seed, GLOBAL_MINIMUM)
+        seq = torch.from_numpy(raw.astype(np.bool_ if _require_bool_result else np.int32))
         bits = seq.tolist()
         if sample_string and not _require_bool_result:
             bits = [''.join(map(str, b)) for b in bits]

@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <random>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -1137,6 +1138,90 @@ template <typename T> static double expect_ops(mpdo_chain_s *ch, const int *site
   return (double)h[0].x;
 }
 
+// Circuit.py:297-446 sample: conditional sampling of the qubits `order`
+// (ascending; the other qubits traced), shots split into groups that share a
+// measured prefix.  The right environments (everything to the right traced)
+// do not depend on the prefix and are built once; the left environment of
+// every group advances one site per step in one batched step (mode 2 gives
+// the x = 0 / 1 projections of all groups), and p(x | prefix) is the full
+// contraction with the right environment, plus the floor `pfloor` on both
+// outcomes as in the reference.  Splits draw binomials from a seeded host
+// generator; bit rows of a group's 1-branch come first.
+template <typename T>
+static void sample_chain(mpdo_chain_s *ch, const int *order, int L, int64_t shots, uint64_t seed, double pfloor,
+                         int8_t *out) {
+  Engine &e = ch->eng->e;
+  check_keep(ch, order, L, ch->n);
+  if (L < 1 || shots < 1) fail(MPDO_ERR_INVALID, "need at least one qubit and one shot");
+  materialize_all<T>(ch);
+  const int n = ch->n;
+  std::memset(out, 0, (size_t)shots * L);
+  // right environments R[k] (l_k x l_k), R[n] = [1]
+  std::vector<DBuf<cx<T>>> R(n + 1);
+  R[n] = DBuf<cx<T>>(e, 1);
+  {
+    const cx<T> one = cmk<T>(T(1), T(0));
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(R[n].p, &one, sizeof(one), cudaMemcpyHostToDevice, e.stream));
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  }
+  // (only R[k + 1] of measured sites k is read)
+  for (int k = n - 1; k > order[0]; --k) {
+    const Site s = ch->s[k];
+    const int rows = s.l * 2 * s.a, ar = 2 * s.a * s.r;
+    DBuf<cx<T>> G(e, (size_t)rows * s.r);
+    gemm<T>(e, rows, s.r, s.r, RM<T>(site_ptr<T>(ch, k), s.r), RM<T>(R[k + 1].p, s.r), G.p, s.r);
+    R[k] = DBuf<cx<T>>(e, (size_t)s.l * s.l);
+    gemm<T>(e, s.l, s.l, ar, RM<T>(G.p, ar), CM<T>(site_ptr<T>(ch, k), ar, 1), R[k].p, s.l);
+  }
+  struct Grp { int64_t start, len; };
+  std::vector<Grp> groups{{0, shots}};
+  std::mt19937_64 rng(seed);
+  Env<T> env = env_start<T>(e);
+  int j = 0;
+  for (int k = 0; k < n && j < L; ++k) {
+    if (order[j] != k) {
+      env_step<T>(e, env, site_ptr<T>(ch, k), ch->s[k], 0, nullptr);
+      continue;
+    }
+    env_step<T>(e, env, site_ptr<T>(ch, k), ch->s[k], 2, nullptr);     // P = 2 G: (group, x)
+    const int G2 = (int)env.P;
+    const int64_t msz = (int64_t)env.r * env.r;
+    DBuf<double> pr(e, G2);
+    env_dot<T>(e.stream, env.E.p, R[k + 1].p, msz, G2, pr.p);
+    std::vector<double> hp(G2);
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(hp.data(), pr.p, G2 * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+    std::vector<Grp> next;
+    std::vector<int> parent;
+    for (size_t g = 0; g < groups.size(); ++g) {
+      const double p0 = hp[2 * g] + pfloor, p1 = hp[2 * g + 1] + pfloor;
+      if (!(p0 >= 0) || !(p1 >= 0))
+        fail(MPDO_ERR_NONFINITE, "State is illegal: conditional probabilities " + std::to_string(p0) + ", " +
+                                     std::to_string(p1));
+      const double q = p1 / (p0 + p1);
+      const int64_t len = groups[g].len;
+      int64_t k1;
+      if (q < pfloor) k1 = 0;
+      else if (q > 1 - pfloor) k1 = len;
+      else k1 = std::binomial_distribution<int64_t>(len, q)(rng);
+      for (int64_t r = 0; r < k1; ++r) out[(size_t)(groups[g].start + r) * L + j] = 1;
+      if (k1 > 0) { next.push_back({groups[g].start, k1}); parent.push_back((int)(2 * g + 1)); }
+      if (len - k1 > 0) { next.push_back({groups[g].start + k1, len - k1}); parent.push_back((int)(2 * g)); }
+    }
+    ++j;
+    if (j == L) break;
+    DBuf<int> idx(e, parent.size());
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(idx.p, parent.data(), parent.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                    e.stream));
+    DBuf<cx<T>> En(e, (size_t)parent.size() * msz);
+    gather_mats<T>(e.stream, env.E.p, En.p, idx.p, msz, (int)parent.size());
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));   // (idx is pageable host data)
+    env.E = std::move(En);
+    env.P = (int64_t)parent.size();
+    groups.swap(next);
+  }
+}
+
 // ------------------------------------------------------------ status ----
 static int *status_slot(Engine &e, int count) {
   if (e.status_used + count > e.status_cap) check_status(e);
@@ -1585,6 +1670,16 @@ mpdo_status mpdo_expect_ops(mpdo_chain_t ch, const int *sites, const double *ops
     set_device(ch->eng);
     if (ch->dtype == MPDO_C64) *out = expect_ops<float>(ch, sites, ops, m);
     else *out = expect_ops<double>(ch, sites, ops, m);
+  });
+}
+
+mpdo_status mpdo_sample(mpdo_chain_t ch, const int *order, int L, int64_t shots, uint64_t seed, double pfloor,
+                        int8_t *bits_out) {
+  return guard([&] {
+    need(ch && order && bits_out, "NULL argument");
+    set_device(ch->eng);
+    if (ch->dtype == MPDO_C64) sample_chain<float>(ch, order, L, shots, seed, pfloor, bits_out);
+    else sample_chain<double>(ch, order, L, shots, seed, pfloor, bits_out);
   });
 }
 

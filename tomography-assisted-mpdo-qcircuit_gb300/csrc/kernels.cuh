@@ -134,6 +134,13 @@ cudaError_t hetrd_cluster(cudaStream_t st, int n, const cx<T> *G, T *d, T *e, cx
 template <typename T>
 void tridiag_top(cudaStream_t st, int n, const T *d, const T *e, int kr, T *lam, cx<T> *Z, T *work, T *tail);
 
+// out[b] = Re sum_i E[b*msize + i] R[i] (left/right environment contraction)
+template <typename T>
+void env_dot(cudaStream_t st, const cx<T> *E, const cx<T> *R, int64_t msize, int batch, double *out);
+// dst[b] = src[idx[b]] (msize-element blocks)
+template <typename T>
+void gather_mats(cudaStream_t st, const cx<T> *src, cx<T> *dst, const int *idx, int64_t msize, int batch);
+
 // Message returned by mpdo_last_error() on the calling thread.
 void set_last_error(const std::string &msg);
 

@@ -257,7 +257,48 @@ __global__ void k_trace(const cx<T> *M, int n, int64_t ld, int64_t bs, int batch
     __syncthreads();
   }
 }
+// out[b] = Re sum_i E[b][i] R[i]  (the full contraction of a left and a
+// right environment, both indexed [ket][bra])
+template <typename T>
+__global__ void k_env_dot(const cx<T> *E, const cx<T> *R, int64_t msize, int batch, double *out) {
+  for (int b = blockIdx.x; b < batch; b += gridDim.x) {
+    __shared__ double red[256];
+    double a = 0;
+    const cx<T> *Eb = E + (int64_t)b * msize;
+    for (int64_t i = threadIdx.x; i < msize; i += blockDim.x) a += (double)Eb[i].x * R[i].x - (double)Eb[i].y * R[i].y;
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[b] = red[0];
+    __syncthreads();
+  }
+}
+
+// dst[b] = src[idx[b]] for msize-element matrices
+template <typename T>
+__global__ void k_gather_mats(const cx<T> *src, cx<T> *dst, const int *idx, int64_t msize, int batch) {
+  const int64_t total = (int64_t)batch * msize;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / msize, i = t % msize;
+    dst[t] = src[(int64_t)idx[b] * msize + i];
+  }
+}
 }  // namespace
+
+template <typename T>
+void env_dot(cudaStream_t st, const cx<T> *E, const cx<T> *R, int64_t msize, int batch, double *out) {
+  k_env_dot<T><<<std::min(batch, 4096), 256, 0, st>>>(E, R, msize, batch, out);
+  count_launch();
+}
+
+template <typename T>
+void gather_mats(cudaStream_t st, const cx<T> *src, cx<T> *dst, const int *idx, int64_t msize, int batch) {
+  k_gather_mats<T><<<nblocks((int64_t)batch * msize), 256, 0, st>>>(src, dst, idx, msize, batch);
+  count_launch();
+}
 
 template <typename T>
 void kraus1q(cudaStream_t st, const cx<T> *A, cx<T> *out, int L, int Aa, int R, const double *g, int K) {
@@ -366,7 +407,9 @@ void sumsq(cudaStream_t st, const cx<T> *x, size_t n, double *out) {
   template void apply_op_site<T>(cudaStream_t, const cx<T> *, cx<T> *, int, int, int, const double *);      \
   template void batched_trace<T>(cudaStream_t, const cx<T> *, int, int64_t, int64_t, int, double2 *);       \
   template void gaussian<T>(cudaStream_t, cx<T> *, size_t, uint64_t);                                     \
-  template void sumsq<T>(cudaStream_t, const cx<T> *, size_t, double *);
+  template void sumsq<T>(cudaStream_t, const cx<T> *, size_t, double *);                                  \
+  template void env_dot<T>(cudaStream_t, const cx<T> *, const cx<T> *, int64_t, int, double *);            \
+  template void gather_mats<T>(cudaStream_t, const cx<T> *, cx<T> *, const int *, int64_t, int);
 INST(float)
 INST(double)
 #undef INST

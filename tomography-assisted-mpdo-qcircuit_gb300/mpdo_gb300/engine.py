@@ -183,6 +183,16 @@ class Chain:
                                       _dptr(out) if report else None))
         return out[: self.n - 1] if report else None
 
+    def sample(self, order: Sequence[int], shots: int, seed: int, pfloor: float = 2.718281828459045e-8) -> np.ndarray:
+        """Conditional sampling of the ascending qubits ``order`` (others
+        traced): shots x len(order) array of 0/1 (int8)."""
+        o = np.ascontiguousarray(np.asarray(order, dtype=np.int32))
+        out = np.zeros((int(shots), len(o)), dtype=np.int8)
+        check(self._lib.mpdo_sample(self.handle, o.ctypes.data_as(C.POINTER(C.c_int)), len(o), int(shots),
+                                    int(seed) & (2 ** 64 - 1), float(pfloor),
+                                    out.ctypes.data_as(C.POINTER(C.c_int8))))
+        return out
+
     def kappa_truncate(self, kappa: Optional[int], max_err: Optional[float]) -> None:
         check(self._lib.mpdo_kappa_truncate(self.handle, int(kappa or 0),
                                             -1.0 if max_err is None else float(max_err)))
