@@ -157,9 +157,20 @@ def evolve_case(S, c, dtype):
     return c
 
 
-def readout(c) -> Dict[str, np.ndarray]:
+# dmOperations.pauli_expect terms pinned with every case (observables as
+# PAULI_DICT indices 0: X, 1: Y, 2: Z, on the given qubits, one list out of
+# order).  dmOperations.expect cannot be pinned: it starts from
+# `Tensor(0.)` (dmOperations.py:141), which current torch rejects.
+PAULI_TERMS = [([2], [0]), ([0, 1], [1, 2]), ([2, 2], [0, 3]), ([1, 0, 2], [3, 0, 1])]
+
+
+def readout(c, S=None) -> Dict[str, np.ndarray]:
     dm = c.cal_dm()
     dims = []
     for node in c.stateNodes:
         dims.append({name: int(node.tensor.shape[i]) for i, name in enumerate(node.axis_names)})
-    return {'dm': dm.detach().cpu().numpy(), 'dims': dims}
+    out = {'dm': dm.detach().cpu().numpy(), 'dims': dims}
+    if S is not None:
+        dmn = c.cal_dmNodes()
+        out['pauli'] = np.array([float(S.dmOperations.pauli_expect(dmn, obs, oqs)) for obs, oqs in PAULI_TERMS])
+    return out

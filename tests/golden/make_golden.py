@@ -11,8 +11,9 @@ by an empty module, as nothing on the evolution path plots.
 For every case the fixture holds: the sequence of gate tensors the reference
 applied (captured when its gate nodes are created; Circuit.py:102 and
 158-166), the truncation markers, the final density matrix (cal_dm), the leg
-dimensions of the final state, and how many SVDs took the randomized branch
-of decompositions.py:112-115.
+dimensions of the final state, dmOperations.pauli_expect values on the
+final state (dmOperations.py:174-201), and how many SVDs took the
+randomized branch of decompositions.py:112-115.
 
 Usage (CPU, needs the reference checkout):
     python tests/golden/make_golden.py [--reference PATH]
@@ -105,7 +106,7 @@ def main():
         gate_nodes.clear()
         with tempfile.TemporaryDirectory() as wd:
             c = evolve_case(S, fn(S, dtype, 'cpu', wd), dtype)
-        out = readout(c)
+        out = readout(c, S)
         ops = _capture_ops(c, gate_nodes)
         flat, meta = [], []
         off = 0
@@ -123,7 +124,8 @@ def main():
                 'ops': meta, 'generator': 'tests/golden/make_golden.py (reference MPDOSimulator on CPU)'}
         path = os.path.join(args.out, f'{name}.npz')
         np.savez_compressed(path, info=np.array(json.dumps(info)), dm=out['dm'].astype(np.complex128),
-                            tensors=np.concatenate(flat) if flat else np.zeros(0, np.complex128))
+                            tensors=np.concatenate(flat) if flat else np.zeros(0, np.complex128),
+                            pauli=out['pauli'])
         print(f'{name}: n={c.qnumber} svd={counts["svd"]} randomized={counts["randomized"]} '
               f'ops={len(meta)} trace={np.trace(out["dm"]).real:.6f} -> {os.path.relpath(path)}')
 

@@ -32,6 +32,12 @@ def load(name):
     return info, ops, z['dm']
 
 
+def pauli_values(name):
+    """dmOperations.pauli_expect of the reference's final state for the terms
+    of cases.PAULI_TERMS."""
+    return np.load(os.path.join(GOLDEN, name + '.npz'))['pauli']
+
+
 def dtype_of(info):
     return torch.complex64 if info['dtype'] == 'complex64' else torch.complex128
 

@@ -13,7 +13,7 @@ import torch
 import golden_io as G
 
 sys.path.insert(0, G.GOLDEN)
-from cases import CASES, evolve_case, readout  # noqa: E402
+from cases import CASES, PAULI_TERMS, evolve_case, readout  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -41,7 +41,7 @@ def test_drop_in_matches_reference(S, name, fused, tmp_path):
     eng = Engine.get(0)
     eng.set_option('fuse_2q', int(fused))
     try:
-        out = readout(evolve_case(S, fn(S, dtype, 'cuda:0', str(tmp_path)), dtype))
+        out = readout(evolve_case(S, fn(S, dtype, 'cuda:0', str(tmp_path)), dtype), S)
     finally:
         eng.set_option('fuse_2q', 1)
     if not fused:
@@ -57,3 +57,4 @@ def test_drop_in_matches_reference(S, name, fused, tmp_path):
         tol = 1e-10
     err = np.abs(out['dm'] - dm_ref).max()
     assert err <= tol, f'max |rho - rho_ref| = {err:.3e}'
+    np.testing.assert_allclose(out['pauli'], G.pauli_values(name), atol=10 * tol)

@@ -38,6 +38,12 @@ def test_oracle_matches_reference(name):
         tol = 1e-10
     err = np.abs(rho - dm_ref).max()
     assert err <= tol * max(1.0, np.abs(dm_ref).max()), f'max |rho - rho_ref| = {err:.3e}'
+    # dmOperations.pauli_expect (dmOperations.py:174-201) on the same state
+    import sys
+    sys.path.insert(0, G.GOLDEN)
+    from cases import PAULI_TERMS
+    got = np.array([float(O.pauli_expect(st, obs, oqs)) for obs, oqs in PAULI_TERMS])
+    np.testing.assert_allclose(got, G.pauli_values(name), atol=tol * 10)
 
 
 def test_fixtures_present():
