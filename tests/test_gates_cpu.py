@@ -1,0 +1,66 @@
+"""The drop-in gate library (MPDOSimulator/QuantumGates) against the
+oracle's gate definitions (which cite QuantumGates/*.py of the reference),
+on the CPU: every gate's matrix, its numpy fast path, and gradients flowing
+through parameterised gates (the reference detaches them; the drop-in keeps
+the angles differentiable)."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import mpdo_oracle as O
+
+ONE = [('IGate', 'I', ()), ('HGate', 'H', ()), ('XGate', 'X', ()), ('YGate', 'Y', ()), ('ZGate', 'Z', ()),
+       ('SGate', 'S', ()), ('SDGGate', 'SDG', ()), ('TGate', 'T', ()), ('RXGate', 'RX', (0.7,)),
+       ('RYGate', 'RY', (1.3,)), ('RZGate', 'RZ', (-2.2,)), ('PGate', 'P', (0.4,)), ('U1Gate', 'U1', (2.5,)),
+       ('U2Gate', 'U2', (0.3, -1.1)), ('U3Gate', 'U3', (0.9, 1.7, -0.6))]
+TWO = [('CNOTGate', 'CNOT', ()), ('CXGate', 'CX', ()), ('CYGate', 'CY', ()), ('CZGate', 'CZ', ()),
+       ('SWAPGate', 'SWAP', ()), ('ISWAPGate', 'ISWAP', ()), ('IIGate', 'II', ()), ('PSWAPGate', 'PSWAP', (0.8,)),
+       ('CPGate', 'CP', (1.9,)), ('RXXGate', 'RXX', (0.5,)), ('RYYGate', 'RYY', (-1.2,)), ('RZZGate', 'RZZ', (2.1,)),
+       ('XXPlusYYGate', 'XXPLUSYY', (0.6, 0.25))]
+
+
+def _cls(name):
+    from MPDOSimulator.QuantumGates import (DoubleGates, PhaseGates, SingleGates, XGates, YGates,  # noqa: F401
+                                            ZGates)
+    for mod in (SingleGates, XGates, YGates, ZGates, PhaseGates, DoubleGates):
+        if hasattr(mod, name):
+            return getattr(mod, name)
+    raise AttributeError(name)
+
+
+@pytest.mark.parametrize('cls,name,params', ONE)
+def test_single_qubit_gates(cls, name, params):
+    g = _cls(cls)(*params, dtype=torch.complex128)
+    ref = O.gate_1q(name, *params).numpy()
+    np.testing.assert_allclose(g.tensor.numpy(), ref, atol=1e-14)
+    np.testing.assert_allclose(g.numpy_tensor() if hasattr(g, 'numpy_tensor') else g.tensor.numpy(), ref, atol=1e-14)
+
+
+@pytest.mark.parametrize('cls,name,params', TWO)
+def test_two_qubit_gates(cls, name, params):
+    g = _cls(cls)(*params, dtype=torch.complex128)
+    ref = O.gate_2q(name, *params).numpy().reshape(2, 2, 2, 2)
+    np.testing.assert_allclose(g.tensor.numpy().reshape(2, 2, 2, 2), ref, atol=1e-14)
+
+
+def test_angles_stay_differentiable():
+    th = torch.tensor(0.8, dtype=torch.float64, requires_grad=True)
+    g = _cls('U3Gate')(th, 0.2, -0.4, dtype=torch.complex128)
+    # the fast path must not be taken for a parameter that needs a gradient
+    np.testing.assert_allclose(g.numpy_tensor(), g.tensor.detach().numpy(), atol=1e-15)
+    loss = (g.tensor.abs() ** 2)[0, 0]                  # cos^2(theta / 2)
+    loss.backward()
+    assert abs(th.grad.item() + math.sin(0.8) / 2) < 1e-12
+
+
+def test_workload_generators():
+    from mpdo_gb300.workloads import config1, config2
+    w = config1()
+    assert (w.n, w.chi, w.kappa, w.gates, w.gate_layers) == (32, 64, 4, 950, 40)
+    for s in range(16):
+        c = config2(s)
+        assert 12 <= c.n <= 40 and c.chi in (16, 32, 64, 128) and c.kappa in (2, 4)
+        assert 10 <= c.depth <= 30 and c.gate_layers == 2 * c.depth
+    assert config2(3).layers == config2(3).layers        # seeded
