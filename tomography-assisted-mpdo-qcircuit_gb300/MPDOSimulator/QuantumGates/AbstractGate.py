@@ -39,6 +39,15 @@ class QuantumGate(ABC, nn.Module):
         self._ideal = ideal
         self.dtype, self.device = dtype, device
 
+    def __setattr__(self, name, value):
+        # gates hold no parameters, buffers or submodules: plain attributes
+        # bypass nn.Module's registration checks, which otherwise dominate the
+        # cost of building circuits of many gates
+        if isinstance(value, nn.Module):
+            nn.Module.__setattr__(self, name, value)
+        else:
+            object.__setattr__(self, name, value)
+
     def _check_Para_Tensor(self, *parameters):
         """AbstractGate.py:42-51 casts angles to the circuit's complex dtype, so
         the trigonometry runs at that precision (an angle given as a float32
