@@ -64,3 +64,31 @@ def test_workload_generators():
         assert 12 <= c.n <= 40 and c.chi in (16, 32, 64, 128) and c.kappa in (2, 4)
         assert 10 <= c.depth <= 30 and c.gate_layers == 2 * c.depth
     assert config2(3).layers == config2(3).layers        # seeded
+
+
+def test_engine_ops_follow_evolve_semantics():
+    # Circuit.py:469-491: gate layers in order, one op per target of a 1q
+    # layer, 2q tensors oriented (min, max), barriers and MeasureZ skipped,
+    # a final kappa pass only when a noisy circuit does not end on truncate
+    import MPDOSimulator as S
+    c = S.TensorCircuit(3, ideal=False, noiseType='idealNoise', chi=4, kappa=2, dtype=torch.complex128,
+                        device='cpu')
+    c.h([0, 2])
+    c.cnot(2, 1)
+    c.barrier()
+    c.truncate()
+    c.measure([0])
+    c.rz(0.3, [1])
+    ops = c._engine_ops()
+    kinds = [o[0] for o in ops]
+    assert kinds == ['1q', '1q', '2q', 'truncate', '1q', 'kappa']
+    assert ops[0][1] == 0 and ops[1][1] == 2 and ops[2][1] == 1
+    assert ops[0][2].shape[:2] == (2, 2) and ops[2][2].shape[:4] == (2, 2, 2, 2)
+    # CNOT with control 2 on the pair (1, 2): oriented to (min, max) legs
+    t = ops[2][2]
+    cnot = O.gate_2q('CNOT').numpy().reshape(2, 2, 2, 2)
+    noisy = np.einsum('ijklp,klmn->ijmnp', np.asarray(c.Noise.dpCTensor2), cnot)    # Circuit.py:91-100
+    np.testing.assert_allclose(t, np.transpose(noisy, (1, 0, 3, 2, 4)), atol=1e-12)
+    ideal = S.TensorCircuit(2, ideal=True, dtype=torch.complex128, device='cpu')
+    ideal.h([0])
+    assert [o[0] for o in ideal._engine_ops()] == ['1q']
