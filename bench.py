@@ -45,7 +45,7 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = json.load(open(os.path.join(ROOT, 'BASELINE.json')))['metric']
+METRIC = 'gates/s & grad-evals/s at n=32 χ=64 κ=4: batched/adjoint vs plain, ≤1e-5 err'
 FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12    # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
 
 
@@ -104,8 +104,8 @@ def allreduce_max(x, ws):
 
 # --------------------------------------------------------------- workload --
 def workload(args, seed=0):
-    from mpdo_gb300.workloads import config1
-    return config1(n=args.n, depth=args.depth, chi=args.chi, kappa=args.kappa, seed=seed)
+    from mpdo_gb300.workloads import u3_brickwork
+    return u3_brickwork(n=args.n, depth=args.depth, chi=args.chi, kappa=args.kappa, seed=seed)
 
 
 def host_ops(w, dtype):

@@ -59,7 +59,7 @@ def _brickwork(c, n: int, depth: int, seed: int, two_q=('CZ', 'CNOT'), truncate_
 
 
 def noisy_err(S, dtype, device, workdir):
-    """idealNoise with the configs' noise model (1q depolarising + amplitude
+    """idealNoise with the benchmark circuits' noise model (1q depolarising + amplitude
     damping, 2q depolarising) at strong rates; no chi cap, a relative
     truncation error 1e-3 (decompositions.py:121-134 rule, exact SVD) and a
     kappa=2 Kraus cap."""

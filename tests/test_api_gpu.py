@@ -37,9 +37,9 @@ def _oracle_ops(w):
 
 
 @pytest.fixture(scope='module')
-def cfg0_oracle():
-    from mpdo_gb300.workloads import config0
-    w = config0()
+def brickwork_oracle():
+    from mpdo_gb300.workloads import ry_rz_cnot_brickwork
+    w = ry_rz_cnot_brickwork()
     ops = _oracle_ops(w)
     st = O.product_state([[1, 0]] * w.n, connected=True)
     O.evolve(st, ops, chi=w.chi, kappa=w.kappa, noisy=True)
@@ -47,12 +47,12 @@ def cfg0_oracle():
 
 
 @pytest.mark.parametrize('dtype,tol', [(torch.complex128, 1e-6), (torch.complex64, 1e-5)])
-def test_config0_matches_oracle(S, cfg0_oracle, dtype, tol):
-    # config 0 (n=8, 8 layers, chi=16, kappa=4): full 256x256 rho and the Z-basis
+def test_small_brickwork_matches_oracle(S, brickwork_oracle, dtype, tol):
+    # the n=8, 8-layer RY/RZ/CNOT brickwork (chi=16, kappa=4): full 256x256 rho and the Z-basis
     # probabilities.  complex128 differs from the oracle only by the split cutoff
     # the fused path skips (tail weight ~1e-8); complex64 within 1e-5.
     from mpdo_gb300.workloads import build_circuit
-    w, ops, ref = cfg0_oracle
+    w, ops, ref = brickwork_oracle
     c = build_circuit(w, dtype=dtype, device='cuda:0')
     c.evolve(S.Tools.create_ket0Series(w.n, dtype=dtype, connected=True))
     rho = c.cal_dm().cpu().numpy()
@@ -98,8 +98,8 @@ def test_depolarizing_known_answer(S):
 
 
 def test_reduced_dm_expect_and_sampling(S):
-    from mpdo_gb300.workloads import config0, build_circuit
-    w = config0(n=5, depth=3, chi=8, kappa=4)
+    from mpdo_gb300.workloads import ry_rz_cnot_brickwork, build_circuit
+    w = ry_rz_cnot_brickwork(n=5, depth=3, chi=8, kappa=4)
     ops = _oracle_ops(w)
     st = O.product_state([[1, 0]] * w.n, connected=True)
     O.evolve(st, ops, chi=w.chi, kappa=w.kappa, noisy=True, cutoff=0.0)

@@ -15,14 +15,14 @@ def mods():
     import mpdo_gb300
     mpdo_gb300.build()
     import MPDOSimulator as S
-    from mpdo_gb300.workloads import build_circuit, config1
-    return S, build_circuit, config1
+    from mpdo_gb300.workloads import build_circuit, u3_brickwork
+    return S, build_circuit, u3_brickwork
 
 
-def _circuits(S, build_circuit, config1, specs):
+def _circuits(S, build_circuit, u3_brickwork, specs):
     out = []
     for n, depth, chi, kappa, seed, dt in specs:
-        w = config1(n=n, depth=depth, chi=chi, kappa=kappa, seed=seed)
+        w = u3_brickwork(n=n, depth=depth, chi=chi, kappa=kappa, seed=seed)
         out.append(build_circuit(w, dtype=dt, device='cuda:0'))
     return out
 
@@ -32,9 +32,9 @@ SPECS = [(6, 3, 8, 2, 0, torch.complex128), (8, 4, 16, 4, 1, torch.complex64), (
 
 
 def test_evolve_batch_equals_single_evolve(mods):
-    S, build_circuit, config1 = mods
-    single = _circuits(S, build_circuit, config1, SPECS)
-    batched = _circuits(S, build_circuit, config1, SPECS)
+    S, build_circuit, u3_brickwork = mods
+    single = _circuits(S, build_circuit, u3_brickwork, SPECS)
+    batched = _circuits(S, build_circuit, u3_brickwork, SPECS)
     for c in single:
         c.evolve(S.Tools.create_ket0Series(c.qnumber, dtype=c.dtype, connected=True))
     states = [S.Tools.create_ket0Series(c.qnumber, dtype=c.dtype, connected=True) for c in batched]
@@ -54,10 +54,10 @@ def test_evolve_batch_equals_single_evolve(mods):
 
 
 def test_batch_runs_many_circuits_on_few_workers(mods):
-    S, build_circuit, config1 = mods
+    S, build_circuit, u3_brickwork = mods
     specs = [(6, 2, 8, 2, s, torch.complex64) for s in range(12)]
-    cs = _circuits(S, build_circuit, config1, specs)
-    ref = _circuits(S, build_circuit, config1, specs)
+    cs = _circuits(S, build_circuit, u3_brickwork, specs)
+    ref = _circuits(S, build_circuit, u3_brickwork, specs)
     res = S.evolve_batch(cs, [S.Tools.create_ket0Series(6, dtype=torch.complex64, connected=True) for _ in cs],
                          workers=3)
     for c, r in zip(ref, res):
@@ -68,7 +68,7 @@ def test_batch_runs_many_circuits_on_few_workers(mods):
 
 def test_batch_failure_stays_with_its_circuit(mods):
     from mpdo_gb300 import Batch
-    S, build_circuit, config1 = mods
+    S, build_circuit, u3_brickwork = mods
     good = dict(n=4, dtype='complex64', vectors=[[1, 0]] * 4, connected=True, chi=4, kappa=2, noisy=True,
                 ops=[('1q', 0, np.eye(2)[:, :, None]), ('2q', 1, np.eye(4).reshape(2, 2, 2, 2)), ('truncate',)],
                 z=True)

@@ -56,14 +56,14 @@ def test_angles_stay_differentiable():
 
 
 def test_workload_generators():
-    from mpdo_gb300.workloads import config1, config2
-    w = config1()
+    from mpdo_gb300.workloads import u3_brickwork, uneven_batch_circuit
+    w = u3_brickwork()
     assert (w.n, w.chi, w.kappa, w.gates, w.gate_layers) == (32, 64, 4, 950, 40)
     for s in range(16):
-        c = config2(s)
+        c = uneven_batch_circuit(s)
         assert 12 <= c.n <= 40 and c.chi in (16, 32, 64, 128) and c.kappa in (2, 4)
         assert 10 <= c.depth <= 30 and c.gate_layers == 2 * c.depth
-    assert config2(3).layers == config2(3).layers        # seeded
+    assert uneven_batch_circuit(3).layers == uneven_batch_circuit(3).layers        # seeded
 
 
 def test_engine_ops_follow_evolve_semantics():

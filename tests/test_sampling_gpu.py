@@ -20,8 +20,8 @@ def S():
 
 
 def _noisy(S, n=6, depth=3, dtype=torch.complex128):
-    from mpdo_gb300.workloads import config1, build_circuit
-    w = config1(n=n, depth=depth, chi=8, kappa=2, seed=5)
+    from mpdo_gb300.workloads import u3_brickwork, build_circuit
+    w = u3_brickwork(n=n, depth=depth, chi=8, kappa=2, seed=5)
     w.noise = dict(p1=0.02, gamma=0.03, p2=0.05)
     c = build_circuit(w, dtype=dtype, device='cuda:0')
     c.evolve(S.Tools.create_ket0Series(n, dtype=dtype, connected=True))

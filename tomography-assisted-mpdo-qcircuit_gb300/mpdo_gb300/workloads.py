@@ -39,7 +39,7 @@ class Workload:
         return sum(1 for L in self.layers if L[0] == 'truncate')
 
 
-def config0(n: int = 8, depth: int = 8, chi: int = 16, kappa: int = 4) -> Workload:
+def ry_rz_cnot_brickwork(n: int = 8, depth: int = 8, chi: int = 16, kappa: int = 4) -> Workload:
     """n=8, 8 brickwork layers of RY(theta), RZ(phi) on every qubit then CNOT on
     even/odd pairs alternating; angles U[0, 2pi) from torch.Generator seed 0
     drawn layer -> sublayer -> qubit in float64."""
@@ -52,10 +52,10 @@ def config0(n: int = 8, depth: int = 8, chi: int = 16, kappa: int = 4) -> Worklo
             layers.append(('truncate',))
         layers += [('2q', 'CNOT', (), q, q + 1) for q in range(L % 2, n - 1, 2)]
         layers.append(('truncate',))
-    return Workload('config0: n=8 depth=8 RY/RZ/CNOT brickwork, chi=16 kappa=4', n, chi, kappa, layers, depth=depth)
+    return Workload(f'n={n} depth={depth} RY/RZ/CNOT brickwork, chi={chi} kappa={kappa}', n, chi, kappa, layers, depth=depth)
 
 
-def config1(n: int = 32, depth: int = 20, chi: int = 64, kappa: int = 4, seed: int = 0) -> Workload:
+def u3_brickwork(n: int = 32, depth: int = 20, chi: int = 64, kappa: int = 4, seed: int = 0) -> Workload:
     """n=32, depth 20: U3 (angles U[0, 2pi)) on every qubit, then CZ or CNOT
     (p = 0.5 each) on brickwork pairs alternating even/odd; seed 0."""
     g = torch.Generator().manual_seed(seed)
@@ -68,11 +68,11 @@ def config1(n: int = 32, depth: int = 20, chi: int = 64, kappa: int = 4, seed: i
         pick = torch.rand(len(pairs), generator=g, dtype=torch.float64).tolist()
         layers += [('2q', 'CZ' if u < 0.5 else 'CNOT', (), q, q + 1) for u, q in zip(pick, pairs)]
         layers.append(('truncate',))
-    return Workload(f'config1: n={n} depth={depth} U3 + CZ/CNOT brickwork, chi={chi} kappa={kappa}', n, chi, kappa,
+    return Workload(f'n={n} depth={depth} U3 + CZ/CNOT brickwork, chi={chi} kappa={kappa}', n, chi, kappa,
                     layers, depth=depth)
 
 
-def config2(seed: int) -> Workload:
+def uneven_batch_circuit(seed: int) -> Workload:
     """One circuit of the uneven batch: n ~ U{12..40}, depth ~ U{10..30},
     chi from {16, 32, 64, 128}, kappa from {2, 4}, drawn from
     torch.Generator seed ``seed``; gates and noise as the n=32 workload (its
@@ -82,7 +82,7 @@ def config2(seed: int) -> Workload:
     depth = int(torch.randint(10, 31, (1,), generator=g))
     chi = (16, 32, 64, 128)[int(torch.randint(0, 4, (1,), generator=g))]
     kappa = (2, 4)[int(torch.randint(0, 2, (1,), generator=g))]
-    w = config1(n=n, depth=depth, chi=chi, kappa=kappa, seed=int(seed))
+    w = u3_brickwork(n=n, depth=depth, chi=chi, kappa=kappa, seed=int(seed))
     w.name = f'uneven batch circuit seed={seed}: n={n} depth={depth} chi={chi} kappa={kappa}'
     return w
 
