@@ -252,6 +252,17 @@ class TensorCircuit(QuantumCircuit):
         return torch.as_tensor(p)
 
     # -------------------------------------------------------- sampling ---
+    def _sample_source(self, nodes):
+        """The chain behind ``nodes`` (Circuit.py:412-413 replicates the given
+        nodes, else the circuit's own state)."""
+        if nodes is None:
+            return self._need_chain()
+        chains = [getattr(n, '_chain', None) for n in nodes]
+        if len(chains) != self.qnumber or chains[0] is None or any(c is not chains[0] for c in chains):
+            raise ValueError('_stateNodes4Sample must be the stateNodes of one evolved state of '
+                             f'{self.qnumber} qubits')
+        return chains[0]
+
     def _conditional_prb(self, chain, order: List[int], history: List[int]) -> float:
         """Circuit.py:297-332: p(1 | history) on qubit order[len(history)],
         the other unmeasured qubits traced, GLOBAL_MINIMUM added to both."""
@@ -275,7 +286,10 @@ class TensorCircuit(QuantumCircuit):
         """Circuit.py:389-446 (batch conditional sampling, 344-387): shots
         sharing a measured prefix form one group; each group's conditional
         probability p(1 | prefix) (GLOBAL_MINIMUM added to both outcomes)
-        splits it binomially."""
+        splits it binomially.  ``_require_sequential_sample`` (the reference's
+        one-shot-at-a-time loop, Circuit.py:334-342) draws from the same
+        distribution, so both run the grouped sampler.  ``_stateNodes4Sample``
+        samples another evolved state (the ``stateNodes`` of a circuit)."""
         shots = shots or 1024
         reduced = reduced or []
         order = [q for q in range(self.qnumber) if q not in reduced]
@@ -283,7 +297,9 @@ class TensorCircuit(QuantumCircuit):
         orientation = orientation or [2] * L
         if len(orientation) != L:
             raise ValueError('Length of orientation must match the sample length. Check reduced or unmeasured qubits.')
-        chain = self._need_chain().clone()
+        chain = self._sample_source(_stateNodes4Sample).clone()
+        if not _tqdm_disable:
+            print(f'Sample Direction:\n (scheme-{"".join("XYZ"[v] for v in orientation)})')
         for val, M in [(0, MeasureX), (1, MeasureY)]:
             idx = [order[i] for i, v in enumerate(orientation) if v == val]
             if idx:
@@ -312,7 +328,8 @@ class TensorCircuit(QuantumCircuit):
                      _stateNodes4Sample=None):
         """Circuit.py:448-466."""
         return [self.sample(shots=shots_per_scheme, orientation=s, reduced=reduced, sample_string=False,
-                            _tqdm_disable=True, _require_bool_result=_require_bool_result, _require_counts=False)
+                            _tqdm_disable=True, _require_bool_result=_require_bool_result, _require_counts=False,
+                            _stateNodes4Sample=_stateNodes4Sample)
                 for s in measurement_schemes]
 
 
