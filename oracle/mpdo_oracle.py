@@ -324,11 +324,26 @@ def svd_truncate(M: torch.Tensor, max_singular_values: Optional[int] = None,
     ``idx`` where ``sqrt(cumsum(s^2))[-1] - sqrt(cumsum(s^2))[idx] <= err`` (121-132).
     ``randomized`` reproduces the patch's switch to the randomized SVD for
     matrices with >= 10000 elements and a singular-value cap (112-115); it is
-    off by default (exact SVD)."""
+    off by default (exact SVD).
+
+    A complex128 ``M`` that requires grad goes through the gradient oracle's
+    truncated SVD (``oracle.adjoint``): the same factors and keep rule, with a
+    backward of its own."""
+    if M.requires_grad and torch.is_grad_enabled() and not randomized:
+        from .adjoint import truncated_svd
+        return truncated_svd(M, max_singular_values, max_truncation_error, relative)
     if randomized and M.numel() >= RANDOMIZED_MIN_NUMEL and max_singular_values is not None:
         u, s, vh = randomized_svd(M, max_singular_values)
     else:
         u, s, vh = _svd(M)
+    keep = keep_count(s, max_singular_values, max_truncation_error, relative)
+    return u[:, :keep], s[:keep], vh[:keep, :], s[keep:]
+
+
+def keep_count(s: torch.Tensor, max_singular_values: Optional[int], max_truncation_error: Optional[float],
+               relative: bool) -> int:
+    """decompositions.py:121-140: how many of the descending singular values
+    ``s`` a split keeps."""
     if max_singular_values is None:
         max_singular_values = s.numel()
     n_err = max_singular_values
@@ -339,8 +354,7 @@ def svd_truncate(M: torch.Tensor, max_singular_values: Optional[int] = None,
             if te[-1] - te[idx] <= thr:
                 n_err = idx + 1
                 break
-    keep = min(max_singular_values, n_err)
-    return u[:, :keep], s[:keep], vh[:keep, :], s[keep:]
+    return min(max_singular_values, n_err)
 
 
 # ----------------------------------------------------------------------------
@@ -454,8 +468,8 @@ def svd_right2left(st: MPDO, chi: Optional[int], max_err: Optional[float],
         _, y, cc, r = b.shape
         m = torch.einsum('lsam,mtcr->lsatcr', a, b).reshape(l * x * aa, y * cc * r)
         u, s, vh, rest = svd_truncate(m, chi, max_err, relative=True, randomized=randomized)
-        tot = float((s ** 2).sum() + (rest ** 2).sum())
-        disc[idx - 1] = float((rest ** 2).sum()) / tot if tot > 0 else 0.0
+        tot = float((s.detach() ** 2).sum() + (rest.detach() ** 2).sum())
+        disc[idx - 1] = float((rest.detach() ** 2).sum()) / tot if tot > 0 else 0.0
         ss = torch.sqrt(s).to(m.dtype)
         k = s.numel()
         st.sites[idx - 1] = (u * ss[None, :]).reshape(l, x, aa, k)
