@@ -25,7 +25,11 @@ autograd, with
   ``(s_j^2 - s_i^2) / ((s_j^2 - s_i^2)^2 + eta)`` so that exactly or nearly
   degenerate pairs (whose numerators vanish for a gauge-invariant loss) stay
   finite;
-* torch's own QR backward for the left-to-right sweep.
+* torch's own QR backward for the left-to-right sweep.  It solves with R^H,
+  so it needs full-rank bonds: a bond that keeps exact zero singular values
+  (the chi cap keeps them whenever it exceeds the rank,
+  decompositions.py:121-140) gives a singular R and NaN gradients.  Full-rank
+  noise channels keep every bond full rank.
 
 Pins: ``tests/test_adjoint_oracle.py`` checks the SVD adjoint against central
 finite differences on random matrices, the untruncated MPDO gradient against
