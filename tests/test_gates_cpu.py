@@ -43,6 +43,55 @@ def test_two_qubit_gates(cls, name, params):
     g = _cls(cls)(*params, dtype=torch.complex128)
     ref = O.gate_2q(name, *params).numpy().reshape(2, 2, 2, 2)
     np.testing.assert_allclose(g.tensor.numpy().reshape(2, 2, 2, 2), ref, atol=1e-14)
+    np.testing.assert_allclose(g.numpy_tensor().reshape(2, 2, 2, 2), ref, atol=1e-14)
+
+
+@pytest.mark.parametrize('cls', ['HGate', 'TGate', 'CNOTGate', 'ISWAPGate'])
+@pytest.mark.parametrize('dtype', [torch.complex64, torch.complex128])
+def test_fixed_gate_fast_path_holds_the_tensor_values(cls, dtype):
+    # the host fast path carries the matrix entries rounded to the circuit
+    # dtype, bit for bit what ``tensor`` holds
+    g = _cls(cls)(dtype=dtype)
+    t = g.tensor.to(torch.complex128).numpy()
+    assert np.array_equal(g.numpy_tensor(), t)
+    assert not g.numpy_tensor().flags.writeable
+
+
+def test_number_angles_stay_on_the_host():
+    # a gate for a CUDA device keeps angles given as numbers in host memory
+    # (no device copy to build, none to read back for the engine); this runs
+    # without CUDA
+    g = _cls('U3Gate')(0.9, 1.7, -0.6, dtype=torch.complex64, device='cuda:0')
+    assert all(p.device.type == 'cpu' and p.dtype == torch.float32 for p in g.para)
+    ref = O.gate_1q('U3', *[float(torch.tensor(x, dtype=torch.float32)) for x in (0.9, 1.7, -0.6)]).numpy()
+    np.testing.assert_allclose(g.numpy_tensor(), ref, atol=1e-15)
+
+
+def test_gate_modules_behave_as_nn_modules():
+    # gates create nn.Module's containers lazily; every module operation
+    # must behave as after nn.Module.__init__, with containers per gate
+    import copy
+    import MPDOSimulator as S
+    c = S.TensorCircuit(3, ideal=False, noiseType='unified', chi=4, kappa=2, device='cpu')
+    c.u3(0.1, 0.2, 0.3, [0])
+    c.cz(0, 1)
+    c.rx(0.4, 2)
+    c.truncate()
+    g0, g1 = c.layers[0], c.layers[1]
+    h = g0.register_forward_hook(lambda *a: None)
+    assert len(g0._forward_hooks) == 1 and len(g1._forward_hooks) == 0
+    h.remove()
+    assert c.to('cpu') is c and c.state_dict() == {} and list(c.named_parameters()) == []
+    c.eval()
+    assert not g0.training
+    c.train()
+    assert g1.training
+    assert len(list(c.modules())) == 6 and 'U3Gate()' in repr(c.layers)
+    d = copy.deepcopy(c)
+    assert abs(d.layers[0].para[0].item() - 0.1) < 1e-7 and d.layers[0] is not g0
+    assert not hasattr(g1, '_build_np')
+    with pytest.raises(AttributeError):
+        g0.no_such_attribute
 
 
 def test_angles_stay_differentiable():

@@ -100,13 +100,13 @@ class TensorCircuit(QuantumCircuit):
     def _noisy_2q(self, gate: QuantumGate) -> np.ndarray:
         """Circuit.py:84-100: idealNoise appends 2q depolarising after the gate;
         realNoise gates (CZEXP/CPEXP) carry their own Kraus leg."""
-        g = gate.tensor
         gnoise = (self.idealNoise and not gate.ideal) or self.realNoise
         if not gnoise or self.realNoise:
-            return self._np(g)
+            return self._gate_np(gate)
         key = None if gate.variational else '2q:' + gate.name
         if key is not None and key in self.noiseTensorDict:
             return self.noiseTensorDict[key]
+        g = gate.tensor
         t = self._np(torch.einsum('ijklp, klmn -> ijmnp', self.Noise.dpCTensor2.to(g.device),
                                   g.to(self.Noise.dpCTensor2.dtype)))
         if key is not None:
@@ -161,7 +161,7 @@ class TensorCircuit(QuantumCircuit):
             if 'truncate' in name:
                 ops.append(('truncate',))
             elif 'barrier' not in name:
-                ops += self._gate_ops(i, self._oqs_list[i])
+                ops += self._gate_ops(i, self._oqs_list[i], layer)
             last = name
         if not self.ideal and last is not None and 'truncate' not in last:          # Circuit.py:487-489
             ops.append(('kappa',))

@@ -8,6 +8,7 @@ two qubits, as in the reference.
 from abc import ABC, abstractmethod
 from typing import Optional
 
+import numpy as np
 import torch
 from torch import Tensor, nn
 
@@ -30,14 +31,46 @@ class Barrier(nn.Module):
         pass
 
 
+_MODULE_STATE = None
+
+
+def _module_state() -> dict:
+    global _MODULE_STATE
+    if _MODULE_STATE is None:
+        _MODULE_STATE = dict(nn.Module().__dict__)
+    return _MODULE_STATE
+
+
+def _module_init(obj: nn.Module) -> None:
+    """``nn.Module.__init__`` for a gate: its flags now, its (empty)
+    parameter / buffer / submodule / hook containers on first access
+    (``QuantumGate.__getattr__``).  A circuit builds one gate module per gate;
+    a dozen fresh containers per gate made the cyclic garbage collector run
+    through the growing circuit over and over, half of the build time."""
+    d = obj.__dict__
+    for k, v in _module_state().items():
+        if not isinstance(v, (dict, set, list)):
+            d[k] = v
+
+
 class QuantumGate(ABC, nn.Module):
     """Base class for quantum gates (AbstractGate.py:31-99)."""
 
     def __init__(self, ideal: Optional[bool] = True, dtype=torch.complex64, device='cpu'):
-        super().__init__()
+        _module_init(self)
         self.para = None
         self._ideal = ideal
         self.dtype, self.device = dtype, device
+
+    def __getattr__(self, name):
+        # nn.Module's per-instance containers, created on first use (each
+        # gate gets its own, as after nn.Module.__init__)
+        proto = _module_state().get(name)
+        if isinstance(proto, (dict, set, list)):
+            value = proto.copy()
+            self.__dict__[name] = value
+            return value
+        return nn.Module.__getattr__(self, name)
 
     def __setattr__(self, name, value):
         # gates hold no parameters, buffers or submodules: plain attributes
@@ -52,14 +85,17 @@ class QuantumGate(ABC, nn.Module):
         """AbstractGate.py:42-51 casts angles to the circuit's complex dtype, so
         the trigonometry runs at that precision (an angle given as a float32
         tensor is widened first).  Angles stay real here, at the matching real
-        precision, which gives the same values and keeps them differentiable."""
+        precision, which gives the same values and keeps them differentiable.
+        An angle given as a number stays in host memory: the engine takes gate
+        matrices from the host, so a device copy would only cost a transfer
+        each way per gate (``tensor`` still returns the matrix on ``device``)."""
         rdt = torch.float64 if self.dtype == torch.complex128 else torch.float32
 
         def conv(p):
             if isinstance(p, Tensor):
                 return p.to(device=self.device, dtype=self.dtype if p.is_complex() else rdt)
             if isinstance(p, (float, int)):
-                return torch.tensor(float(p), dtype=rdt, device=self.device)
+                return torch.tensor(float(p), dtype=rdt)
             raise ValueError(f'Invalid type for gate parameter: {type(p)}')
         ps = [conv(p) for p in parameters]
         return ps if len(parameters) > 1 else ps[0]
@@ -147,6 +183,21 @@ class _Fixed(QuantumGate):
     def tensor(self):
         t = torch.tensor(self._DATA, dtype=self.dtype, device=self.device)
         return t if self._SINGLE else t.reshape(2, 2, 2, 2)
+
+    _NP_CACHE = {}
+
+    def numpy_tensor(self):
+        """The matrix as complex128 numpy, its entries rounded to ``dtype``
+        (the values ``tensor`` holds), built once per gate class and dtype."""
+        key = (type(self), self.dtype)
+        t = _Fixed._NP_CACHE.get(key)
+        if t is None:
+            np_dt = np.complex64 if self.dtype == torch.complex64 else np.complex128
+            t = np.asarray(self._DATA, dtype=np_dt).astype(np.complex128)
+            t = t if self._SINGLE else t.reshape(2, 2, 2, 2)
+            t.setflags(write=False)
+            _Fixed._NP_CACHE[key] = t
+        return t
 
     @property
     def rank(self):
