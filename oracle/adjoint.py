@@ -28,8 +28,11 @@ autograd, with
 * torch's own QR backward for the left-to-right sweep.  It solves with R^H,
   so it needs full-rank bonds: a bond that keeps exact zero singular values
   (the chi cap keeps them whenever it exceeds the rank,
-  decompositions.py:121-140) gives a singular R and NaN gradients.  Full-rank
-  noise channels keep every bond full rank.
+  decompositions.py:121-140) gives a singular R and NaN gradients.  The
+  differentiated splits therefore keep at most the numerical rank
+  (singular values above RANK_TOL * s_0): the state changes by rounding-level
+  amounts only (|s| < 1e-13 s_0 in the dropped directions) and every bond
+  stays full rank.
 
 Pins: ``tests/test_adjoint_oracle.py`` checks the SVD adjoint against central
 finite differences on random matrices, the untruncated MPDO gradient against
@@ -49,6 +52,8 @@ from . import mpdo_oracle as O
 
 # relative broadening of the 1/(s_j^2 - s_i^2) terms: eta = (BROADENING s_0^2)^2
 BROADENING = 1e-12
+# singular values below RANK_TOL * s_0 are dropped from differentiated splits
+RANK_TOL = 1e-13
 
 
 def _inv(s: torch.Tensor) -> torch.Tensor:
@@ -63,6 +68,12 @@ class _TruncatedSVD(torch.autograd.Function):
         dt = M.dtype
         u, s, vh = O._svd128(M.detach().to(torch.complex128))
         k = O.keep_count(s, max_sv, max_err, relative)
+        if RANK_TOL > 0 and k > 1:
+            # numerical rank: singular values at the rounding level of s_0 are
+            # zeros of the exact factorisation; keeping them (the chi cap
+            # does whenever it exceeds the rank) would hand the next QR a
+            # singular R, where its adjoint is undefined
+            k = max(1, min(k, int((s > RANK_TOL * s[0]).sum())))
         ctx.save_for_backward(u, s, vh)
         ctx.k, ctx.dt, ctx.broadening = k, dt, broadening
         rdt = torch.float64 if dt == torch.complex128 else torch.float32

@@ -114,12 +114,14 @@ def fit(circuits: List[torch.Tensor], data: List[torch.Tensor], chi: int, kappa:
         lr: float = 0.02, K_true: Optional[torch.Tensor] = None, init_seed: int = 1,
         init_eps: float = 1e-2) -> Dict[str, list]:
     """Adam on W (16 x 4 complex) minimising sum_c || <Z>_c(stiefel(W)) -
-    data_c ||^2.  W starts at the identity channel moved by ``init_eps``
-    (``hidden_isometry(init_seed, init_eps)``): with three Kraus operators
-    exactly zero the bonds carry exact zero singular values (the chi cap keeps
-    them, decompositions.py:121-140), the next QR factor R is singular and
-    the QR adjoint (R^-H solves) is undefined.  Returns the loss per step
-    (before the update) and, with ``K_true``, the diamond-norm proxy."""
+    data_c ||^2.  W starts at ``hidden_isometry(init_seed, init_eps)``, the
+    identity channel moved by ``init_eps``.  The exact identity
+    (``init_eps = 0``) runs -- the gradient oracle keeps the numerical rank
+    of its rank-deficient bonds -- but it is a stationary point of every
+    dissipative direction: rho depends on the three zero Kraus operators
+    quadratically, so their gradient vanishes there and Adam could only fit
+    a unitary.  Returns the loss per step (before the update) and, with
+    ``K_true``, the diamond-norm proxy."""
     W = hidden_isometry(seed=init_seed, eps=init_eps).clone().requires_grad_(True)
     opt = torch.optim.Adam([W], lr=lr)
     hist = {'loss': [], 'proxy': []}

@@ -2,6 +2,8 @@
 hidden channel is CPTP, the Choi-matrix proxy behaves as a distance, the
 fit loss's gradient through the realNoise 2q path matches central finite
 differences, and a short Adam run lowers the loss."""
+import math
+
 import torch
 
 from oracle import channel_fit as C
@@ -51,5 +53,18 @@ def test_short_fit_lowers_the_loss():
     circs = [C.random_circuit(N, DEPTH, s) for s in range(4)]
     data = [C.marginals(a, K_true, CHI, KAPPA) for a in circs]
     h = C.fit(circs, data, CHI, KAPPA, steps=8, lr=0.02, K_true=K_true)
-    assert h['loss'][-1] < h['loss'][0] / 5
+    assert all(map(math.isfinite, h['loss'])) and h['loss'][-1] < h['loss'][0] / 5
     assert all(0 <= p < 1 for p in h['proxy'])
+
+
+def test_identity_start_is_stationary_for_dissipative_directions():
+    # at the exact identity channel the three zero Kraus operators enter rho
+    # quadratically: their gradient vanishes (the bonds there are rank
+    # deficient, which the gradient oracle handles by keeping the numerical rank)
+    K_true = C.kraus(C.hidden_isometry(7, 0.05))
+    circs = [C.random_circuit(N, DEPTH, s) for s in range(2)]
+    data = [C.marginals(a, K_true, CHI, KAPPA) for a in circs]
+    W = C.hidden_isometry(1, 0.0).clone().requires_grad_(True)
+    _loss(W, circs, data).backward()
+    assert torch.isfinite(W.grad).all()
+    assert W.grad[:4].abs().max() > 1e-3 and W.grad[4:].abs().max() < 1e-12
