@@ -17,7 +17,8 @@ import torch
 from torch import Tensor
 
 __all__ = ['create_ket0Series', 'create_ket1Series', 'create_ketPlusSeries', 'create_ketMinusSeries',
-           'create_ketRandomSeries', 'create_ketHadamardSeries', 'plot_histogram', 'density2prob',
+           'create_ketRandomSeries', 'create_ketHadamardSeries', 'plot_histogram', 'plot_histogram_multiBars',
+           'density2prob',
            'select_device', 'tc_expect', 'EdgeName2AxisName', 'count_item', 'cal_fidelity',
            'random_measurementScheme', 'QubitNode']
 
@@ -153,6 +154,11 @@ def density2prob(rho_in: Tensor, bases: Optional[Dict] = None, tol: Optional[flo
 def plot_histogram(*args, **kwargs):
     """Plotting needs matplotlib, which is not part of this engine."""
     raise ImportError('plot_histogram needs matplotlib; plotting is not part of the GB300 engine')
+
+
+def plot_histogram_multiBars(*args, **kwargs):
+    """Tools.py:339-449 plots with matplotlib, which is not part of this engine."""
+    raise ImportError('plot_histogram_multiBars needs matplotlib; plotting is not part of the GB300 engine')
 
 
 def select_device(device: Optional[Union[str, int]] = None):
