@@ -3,7 +3,6 @@ own restatement of the reference's gate and noise builders)."""
 import math
 import random
 
-import torch
 
 from oracle import mpdo_oracle as O
 

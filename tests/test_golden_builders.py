@@ -6,7 +6,6 @@ drop-in package builds the same circuits from the same API calls; every
 applied operation must be the same quantum operation (compared as the
 superoperator sum_k K_k (x) conj(K_k), which does not depend on the order or
 phases of the Kraus operators)."""
-import os
 import sys
 
 import numpy as np

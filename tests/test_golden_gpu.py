@@ -13,7 +13,7 @@ import torch
 import golden_io as G
 
 sys.path.insert(0, G.GOLDEN)
-from cases import CASES, PAULI_TERMS, evolve_case, readout  # noqa: E402
+from cases import CASES, evolve_case, readout  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 

@@ -1,6 +1,5 @@
 """CPU checks of the oracle: physics pins against the dense simulator and
 analytic known answers (no GPU)."""
-import math
 
 import numpy as np
 import pytest

@@ -9,12 +9,10 @@ follows when the last layer is not a truncate.  Every contraction and
 factorisation runs on the GPU through ``libmpdo_gb300.so``; there is no CPU
 path.
 """
-import math
-from typing import Any, Dict, List, Optional, Tuple, Union
+from typing import Any, Dict, List, Optional, Union
 
 import numpy as np
 import torch
-from torch.linalg import LinAlgError
 
 from .AbstractCircuit import QuantumCircuit
 from .NoiseChannel import NoiseChannel

@@ -1,7 +1,7 @@
 """Single-qubit gates (reference: QuantumGates/SingleGates.py)."""
 import cmath
 import math
-from typing import Optional, Union
+from typing import Optional
 from warnings import warn
 
 import numpy as np

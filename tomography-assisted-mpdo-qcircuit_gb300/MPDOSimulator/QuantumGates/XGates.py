@@ -1,5 +1,4 @@
 """X-family gates (reference: QuantumGates/XGates.py)."""
-import cmath
 import math
 from typing import Optional
 

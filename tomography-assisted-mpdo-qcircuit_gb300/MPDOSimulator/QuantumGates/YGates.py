@@ -1,5 +1,4 @@
 """Y-family gates (reference: QuantumGates/YGates.py)."""
-import cmath
 import math
 from typing import Optional
 

@@ -1,6 +1,5 @@
 """Z-family gates (reference: QuantumGates/ZGates.py)."""
 import cmath
-import math
 from typing import Optional
 
 import numpy as np

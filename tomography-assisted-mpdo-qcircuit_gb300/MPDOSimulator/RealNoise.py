@@ -1,6 +1,5 @@
 """Experimental process (chi) matrix -> Kraus tensor of a noisy two-qubit gate
 (reference: MPDOSimulator/RealNoise.py)."""
-import itertools
 import os
 from typing import Dict, List, Optional, Union
 

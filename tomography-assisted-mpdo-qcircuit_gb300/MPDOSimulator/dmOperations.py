@@ -4,7 +4,7 @@
 keeps the GPU chain and the set of qubits whose physical legs are traced.
 All contractions run on the GPU through the engine's environment sweeps.
 """
-from typing import List, Optional, Tuple, Union
+from typing import List, Optional, Union
 
 import numpy as np
 import torch
