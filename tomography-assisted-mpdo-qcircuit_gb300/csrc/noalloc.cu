@@ -62,7 +62,6 @@ struct Carve {
     off += n * sizeof(X);
     return p;
   }
-  bool ok() const { return off <= cap; }
 };
 
 struct Level {
