@@ -141,3 +141,42 @@ def test_engine_ops_follow_evolve_semantics():
     ideal = S.TensorCircuit(2, ideal=True, dtype=torch.complex128, device='cpu')
     ideal.h([0])
     assert [o[0] for o in ideal._engine_ops()] == ['1q']
+
+
+class _FakeChain:
+    """Records the engine calls the TNNOptimizer entry points make."""
+
+    def __init__(self, n, bonds=True):
+        self.n, self.bonds, self.calls = n, bonds, []
+
+    def bond_present(self, b):
+        return self.bonds
+
+    def truncate(self, *a):
+        self.calls.append(('truncate',) + a)
+
+    def kappa_truncate(self, *a):
+        self.calls.append(('kappa',) + a)
+
+
+def test_tnnoptimizer_entry_points_map_to_engine_operations():
+    # TNNOptimizer.py:51-197 on the nodes of an evolved state
+    from MPDOSimulator import TNNOptimizer as T, Tools
+    ch = _FakeChain(3)
+    nodes = [Tools.QubitNode(None, f'qubit_{k}', [], chain=ch, index=k) for k in range(3)]
+    assert T.bondTruncate(nodes) is None and T.svdKappa_left2right(nodes) is None and ch.calls == []
+    T.bondTruncate(nodes, 8)
+    T.bondTruncate(nodes, None, 1e-3)
+    T.svdKappa_left2right(nodes, 4, 1e-3)
+    assert ch.calls == [('truncate', 8, None, None, False), ('truncate', None, None, 1e-3, False),
+                        ('kappa', 4, 1e-3)]
+    assert T.checkConnectivity(nodes) and not T.checkConnectivity(
+        [Tools.QubitNode(None, f'q{k}', [], chain=_FakeChain(2, bonds=False), index=k) for k in range(1)] * 2)
+    assert not T.checkConnectivity(Tools.create_ket0Series(3)) and T.checkConnectivity(
+        Tools.create_ket0Series(3, connected=True))
+    with pytest.raises(TypeError):
+        T.bondTruncate(tuple(nodes), 4)
+    with pytest.raises(ValueError):
+        T.bondTruncate(nodes[:2], 4)
+    with pytest.raises(NotImplementedError):
+        T.qr_left2right(nodes)
