@@ -142,6 +142,83 @@ def real_noise(S, dtype, device, workdir):
     return c
 
 
+def gate_zoo(S, dtype, device, workdir):
+    """idealNoise (the 'medium' chip's 1q channels replaced by the benchmark
+    circuits' noise model) over every gate method of the API: fixed and
+    parameterised 1q gates, an arbitrary 1q matrix, noisy fixed 2q gates in
+    both orientations and parameterised 2q gates (ideal: the reference's
+    idealNoise path fails on noisy parameterised 2q gates, AbstractGate axis
+    names), truncate after every sublayer, relative error cap 1e-7."""
+    c = S.TensorCircuit(4, ideal=False, noiseType='idealNoise', chi=None, kappa=4, max_truncation_err=1e-7,
+                        chip='medium', dtype=dtype, device=device)
+    _override_noise(c, 0.02, 0.03, 0.04, dtype)
+    _connect(c, 4)
+    c.h([0, 3])
+    c.x([1])
+    c.y([2])
+    c.truncate()
+    c.z([0])
+    c.s([1])
+    c.sdg([2])
+    c.t([3])
+    c.truncate()
+    c.rx(0.7, [0])
+    c.ry(1.3, [1])
+    c.rz(-2.2, [2])
+    c.p(0.4, [3])
+    c.u1(2.5, [0])
+    c.u3(0.9, 1.7, -0.6, [1])
+    th = 0.8
+    arb = torch.tensor([[math.cos(th), -math.sin(th)], [math.sin(th), math.cos(th)]], dtype=dtype)
+    c.arbSingle(arb, [2])
+    c.truncate()
+    c.cy(1, 0)
+    c.swap(2, 3)
+    c.truncate()
+    c.iswap(1, 2)
+    c.ii(0, 1, True)
+    c.truncate()
+    c.cx(3, 2)
+    c.rxx(0.5, 0, 1, True)
+    c.truncate()
+    c.ryy(-1.2, 1, 2, True)
+    c.rzz(2.1, 2, 3, True)
+    c.truncate()
+    c.pswap(0.8, 0, 1, True)
+    c.cp(1.9, 3, 2, True)
+    c.truncate()
+    c.xx_yy(0.6, 0.25, 1, 2, True)
+    c.truncate()
+    return c
+
+
+def real_noise_cp(S, dtype, device, workdir):
+    """noiseType='realNoise' with CP gates, whose Kraus set comes from a CP
+    chi matrix (AbstractCircuit.py:404-421, RealNoise.py cpExp_channel), and
+    the 'best' chip's 1q channels."""
+    rng = np.random.default_rng(16)
+    g = 0.12 * (rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16)))
+    g[0, 0] += 1.0
+    chi = g @ g.conj().T
+    chi /= np.trace(chi).real
+    fn = os.path.join(workdir, 'chi_cp_synthetic.npz')
+    np.savez(fn, chi=chi)
+    files = {'CZ': {}, 'CP': {'01': fn, '12': fn, '23': fn}}
+    c = S.TensorCircuit(4, ideal=False, noiseType='realNoise', chiFileDict=files, chi=None, kappa=4,
+                        max_truncation_err=1e-8, chip='best', dtype=dtype, device=device)
+    for q in range(4):
+        c.h([q])
+    c.truncate()
+    c.cp(None, 0, 1)
+    c.cp(None, 3, 2)
+    c.truncate()
+    c.cp(None, 2, 1)
+    c.truncate()
+    c.rx(0.4, [0, 1, 2, 3])
+    c.truncate()
+    return c
+
+
 CASES = {
     'noisy_err_c128': (noisy_err, torch.complex128),
     'noisy_err_c64': (noisy_err, torch.complex64),
@@ -149,6 +226,16 @@ CASES = {
     'ideal_chi_c128': (ideal_chi, torch.complex128),
     'unified_chip_c128': (unified_chip, torch.complex128),
     'real_noise_c128': (real_noise, torch.complex128),
+}
+
+# Cases pinned on the CPU only: the drop-in API builds the reference's
+# operations (tests/test_golden_builders.py) and the oracle reproduces the
+# reference's density matrix from them (tests/test_golden_oracle.py).  The
+# engine runs such operations through the same entry points as CASES; these
+# were added after the last GPU run and have not been through the GPU tests.
+HOST_CASES = {
+    'gate_zoo_c128': (gate_zoo, torch.complex128),
+    'real_noise_cp_c128': (real_noise_cp, torch.complex128),
 }
 
 

@@ -75,6 +75,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE', '/root/reference'))
     ap.add_argument('--out', default=HERE)
+    ap.add_argument('--only', default='', help='comma-separated case names (default: all)')
     args = ap.parse_args()
     tn, D = _install(args.reference)
     counts = {'svd': 0, 'randomized': 0}
@@ -99,9 +100,12 @@ def main():
 
     tn.Node.__init__ = init
     import MPDOSimulator as S
-    from cases import CASES, evolve_case, readout
+    from cases import CASES, HOST_CASES, evolve_case, readout
     torch.manual_seed(0)
-    for name, (fn, dtype) in CASES.items():
+    only = set(filter(None, args.only.split(',')))
+    for name, (fn, dtype) in {**CASES, **HOST_CASES}.items():
+        if only and name not in only:
+            continue
         counts.update(svd=0, randomized=0)
         gate_nodes.clear()
         with tempfile.TemporaryDirectory() as wd:

@@ -15,7 +15,9 @@ import torch
 import golden_io as G
 
 sys.path.insert(0, G.GOLDEN)
-from cases import CASES  # noqa: E402
+from cases import CASES, HOST_CASES  # noqa: E402
+
+ALL_CASES = {**CASES, **HOST_CASES}
 
 
 def _drop_in_ops(c):
@@ -46,10 +48,10 @@ def _superop(t, n_out):
     return np.einsum('ijk,lmk->iljm', k, k.conj()).reshape(d * d, d * d)
 
 
-@pytest.mark.parametrize('name', sorted(CASES))
+@pytest.mark.parametrize('name', sorted(ALL_CASES))
 def test_drop_in_builds_reference_operations(name, tmp_path):
     import MPDOSimulator as S
-    fn, dtype = CASES[name]
+    fn, dtype = ALL_CASES[name]
     c = fn(S, dtype, 'cpu', str(tmp_path))
     info, ref_ops, _ = G.load(name)
     mine = _drop_in_ops(c)
