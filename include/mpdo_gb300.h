@@ -234,6 +234,15 @@ mpdo_status mpdo_debug_qr(mpdo_engine_t eng, int dtype, int m, int n, const doub
 mpdo_status mpdo_debug_svd(mpdo_engine_t eng, int dtype, int m, int n, const double *a, double *w,
                            double *sigma);
 
+/* The truncation rule every SVD step applies to its singular values
+ * (decompositions.py:121-140; the split's absolute cutoff, Circuit.py:123,
+ * and the sweeps' relative error, TNNOptimizer.py:124-129): how many of the
+ * descending values s[0..len) of a matrix with nsv singular values (entries
+ * len..nsv-1 are zero) are kept under the cap max_sv and the error rule
+ * (err < 0: no error rule; relative != 0: threshold err * s[0]).  Host code
+ * only; needs no device. */
+mpdo_status mpdo_keep_count(const double *s, int len, int nsv, int max_sv, double err, int relative, int *keep);
+
 /* Allocation-free SVD step (no counterpart in the reference).  For callers
  * that cannot allocate device memory -- a process whose device memory is
  * pre-partitioned by its own allocator, or code under an allocation hook that

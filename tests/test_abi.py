@@ -1,5 +1,7 @@
 """The C-ABI library loads, exports every entry point of include/mpdo_gb300.h
-and fails loudly (no CPU fallback) where no GPU is present.  No compute."""
+and fails loudly (no CPU fallback) where no GPU is present.  No device
+compute; the engine's host-side truncation rule is checked against the
+oracle's."""
 import re
 from pathlib import Path
 
@@ -78,3 +80,36 @@ def test_batch_arguments_checked_before_any_device_work(lib):
     assert b'workers' in lib.mpdo_last_error()
     assert lib.mpdo_batch_run(None, 1, None, None, None, None) == _lib.MPDO_ERR_INVALID
     assert lib.mpdo_batch_error(None, 0) == b''
+
+
+def test_engine_truncation_rule_matches_the_oracle(lib):
+    # decompositions.py:121-140 as the engine applies it on the host (split
+    # cutoff and sweep error rule) against the oracle's keep_count, on random
+    # graded spectra, with zero-extended spectra (nsv > len), exact ties at
+    # the cut and caps; needs no device
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from oracle import mpdo_oracle as O
+    rng = np.random.default_rng(0)
+    out = C.c_int()
+    cases = 0
+    for trial in range(400):
+        ln = int(rng.integers(1, 40))
+        s = np.sort(np.exp(rng.uniform(-25, 0, ln)))[::-1].copy()
+        if trial % 7 == 0:
+            s[ln // 2:] = 0.0
+        if trial % 11 == 0 and ln > 3:
+            s[1:3] = s[1]
+        nsv = ln + int(rng.integers(0, 5))
+        for max_sv in (nsv, max(1, ln // 2), 1):
+            for err, rel in ((-1.0, 0), (2.718281828459045e-8, 0), (1e-3, 1), (1e-7, 1), (0.5, 1)):
+                assert lib.mpdo_keep_count(s.ctypes.data_as(C.POINTER(C.c_double)), ln, nsv, max_sv, err, rel,
+                                           C.byref(out)) == 0
+                full = torch.from_numpy(np.concatenate([s, np.zeros(nsv - ln)]))
+                want = O.keep_count(full, max_sv, None if err < 0 else err, bool(rel))
+                assert out.value == want, (trial, ln, nsv, max_sv, err, rel, out.value, want)
+                cases += 1
+    assert cases == 400 * 15

@@ -1726,6 +1726,14 @@ mpdo_status mpdo_debug_split(mpdo_engine_t eng, int dtype, int m, int n, int kee
   });
 }
 
+mpdo_status mpdo_keep_count(const double *s, int len, int nsv, int max_sv, double err, int relative, int *keep) {
+  return guard([&] {
+    need(keep != nullptr && (s != nullptr || len == 0) && len >= 0 && nsv >= 0 && max_sv >= 0, "bad argument");
+    const std::vector<double> v(s, s + len);
+    *keep = error_rule_keep<double>(v, nsv, max_sv, err, relative != 0);
+  });
+}
+
 mpdo_status mpdo_debug_svd(mpdo_engine_t eng, int dtype, int m, int n, const double *a, double *w,
                            double *sigma) {
   return guard([&] {

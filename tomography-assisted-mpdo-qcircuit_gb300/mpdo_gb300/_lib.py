@@ -72,6 +72,7 @@ SIGNATURES = {
     'mpdo_debug_qr': (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_debug_svd': (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_debug_split': (_I, [_P, _I, _I, _I, _I, _DP, _DP, _DP]),
+    'mpdo_keep_count': (_I, [_DP, _I, _I, _I, C.c_double, _I, _IP]),
     'mpdo_right_svd_noalloc': (_I, [_I, _I, _P, _P, _P, _P, _P]),
     'mpdo_batch_create': (_I, [_I, _I, C.POINTER(_P)]),
     'mpdo_batch_destroy': (_I, [_P]),
