@@ -92,6 +92,8 @@ def test_gate_modules_behave_as_nn_modules():
     assert not hasattr(g1, '_build_np')
     with pytest.raises(AttributeError):
         g0.no_such_attribute
+    g1.extra = torch.nn.Identity()                  # a submodule still registers
+    assert 'extra' in dict(g1.named_children()) and len(list(c.modules())) == 7
 
 
 def test_angles_stay_differentiable():

@@ -77,6 +77,7 @@ class QuantumGate(ABC, nn.Module):
         # bypass nn.Module's registration checks, which otherwise dominate the
         # cost of building circuits of many gates
         if isinstance(value, nn.Module):
+            self._modules                    # noqa: B018 -- create the container nn.Module registers into
             nn.Module.__setattr__(self, name, value)
         else:
             object.__setattr__(self, name, value)
