@@ -233,7 +233,18 @@ CASES = {
 # reference's density matrix from them (tests/test_golden_oracle.py).  The
 # engine runs such operations through the same entry points as CASES; these
 # were added after the last GPU run and have not been through the GPU tests.
+def unified_medium(S, dtype, device, workdir):
+    """noiseType='unified' with the 'medium' chip's decay and dephasing
+    channels (ChipInfo.py, NoiseChannel.py:144-170) on every 1q gate."""
+    c = S.TensorCircuit(4, ideal=False, noiseType='unified', chi=3, kappa=2, chip='medium', dtype=dtype,
+                        device=device)
+    _connect(c, 4)
+    _brickwork(c, 4, 2, seed=17)
+    return c
+
+
 HOST_CASES = {
+    'unified_medium_c128': (unified_medium, torch.complex128),
     'gate_zoo_c128': (gate_zoo, torch.complex128),
     'real_noise_cp_c128': (real_noise_cp, torch.complex128),
 }

@@ -119,3 +119,21 @@ def test_chi_to_kraus_reproduces_ideal_cz():
     k = t[..., 0].reshape(4, 4).numpy()
     ph = k[0, 0] / abs(k[0, 0])
     np.testing.assert_allclose(k / ph, cz, atol=1e-12)
+
+
+def test_expect_dense_against_the_dense_simulator():
+    # dmOperations.py:135-171: Tr(rho_oq . O) for a two-qubit observable given
+    # on qubits listed out of order (no truncation binds: rho is exact)
+    n = 3
+    ops = brickwork(n, 2, seed=21)
+    st = O.product_state([[1, 0]] * n, connected=True)
+    O.evolve(st, ops, chi=8, kappa=8, noisy=True)
+    rho = D.run(n, ops)
+    g = torch.Generator().manual_seed(3)
+    a = torch.complex(torch.randn(4, 4, dtype=torch.float64, generator=g),
+                      torch.randn(4, 4, dtype=torch.float64, generator=g))
+    obs = (a + a.conj().T).reshape(2, 2, 2, 2)            # [out q2, out q0, in q2, in q0]
+    eye = torch.eye(2, dtype=torch.complex128)
+    full = torch.einsum('xyuv,pq->ypxvqu', obs, eye).reshape(8, 8)   # rows (s0, s1, s2), columns (t0, t1, t2)
+    want = torch.trace(rho @ full).real.item()
+    assert abs(O.expect_dense(st, obs.reshape(4, 4), [2, 0]).item() - want) < 1e-12
