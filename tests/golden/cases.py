@@ -148,7 +148,8 @@ def gate_zoo(S, dtype, device, workdir):
     parameterised 1q gates, an arbitrary 1q matrix, noisy fixed 2q gates in
     both orientations and parameterised 2q gates (ideal: the reference's
     idealNoise path fails on noisy parameterised 2q gates, AbstractGate axis
-    names), truncate after every sublayer, relative error cap 1e-7."""
+    names), then X / Y measurement basis changes and a reset, truncate after
+    every sublayer, relative error cap 1e-7."""
     c = S.TensorCircuit(4, ideal=False, noiseType='idealNoise', chi=None, kappa=4, max_truncation_err=1e-7,
                         chip='medium', dtype=dtype, device=device)
     _override_noise(c, 0.02, 0.03, 0.04, dtype)
@@ -188,6 +189,9 @@ def gate_zoo(S, dtype, device, workdir):
     c.cp(1.9, 3, 2, True)
     c.truncate()
     c.xx_yy(0.6, 0.25, 1, 2, True)
+    c.truncate()
+    c.measure([0, 2], [0, 1])
+    c.reset1([3])
     c.truncate()
     return c
 
