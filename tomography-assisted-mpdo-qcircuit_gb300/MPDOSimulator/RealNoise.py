@@ -55,6 +55,10 @@ def noisyTensor(chi, gate_factor: Optional[Dict] = None, dtype=torch.complex64,
 
 
 def _exp_channel(filename, dtype, device):
+    if not os.path.exists(filename):
+        raise FileNotFoundError(f'chi-matrix file {filename!r} not found; the measured default chi matrices '
+                                '(chi/czDefault.mat, chi/cpDefault.mat) are the reference\'s data and do not '
+                                'ship with this package: pass the file (chiFileDict / filename=)')
     chi = readExpChi(filename=filename)
     t = torch.stack(noisyTensor(chi))
     return torch.einsum('ijlmn -> jlmni', t).to(dtype=dtype, device=device)
