@@ -247,7 +247,19 @@ def unified_medium(S, dtype, device, workdir):
     return c
 
 
+def unified_best(S, dtype, device, workdir):
+    """noiseType='unified' with the 'best' chip: zero bath rate, so its decay
+    and dephasing Kraus sets carry exactly-zero operators (rank-deficient
+    Kraus legs for the kappa pass)."""
+    c = S.TensorCircuit(4, ideal=False, noiseType='unified', chi=4, kappa=2, chip='best', dtype=dtype,
+                        device=device)
+    _connect(c, 4)
+    _brickwork(c, 4, 2, seed=18)
+    return c
+
+
 HOST_CASES = {
+    'unified_best_c128': (unified_best, torch.complex128),
     'unified_medium_c128': (unified_medium, torch.complex128),
     'gate_zoo_c128': (gate_zoo, torch.complex128),
     'real_noise_cp_c128': (real_noise_cp, torch.complex128),
