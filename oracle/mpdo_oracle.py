@@ -607,6 +607,27 @@ def expect_dense(st: MPDO, obs: torch.Tensor, oq: Sequence[int]) -> torch.Tensor
     return torch.trace(rho @ o).real
 
 
+_PROJ = [torch.tensor([[1, 0], [0, 0]], dtype=torch.complex128), torch.tensor([[0, 0], [0, 1]], dtype=torch.complex128)]
+
+
+def conditional_p1(st: MPDO, order: Sequence[int], history: Sequence[int]) -> float:
+    """Circuit.py:297-332: the probability that qubit ``order[len(history)]``
+    reads 1 given that ``order[:len(history)]`` read ``history``, every other
+    qubit traced: the two unnormalised outcome weights, each plus
+    GLOBAL_MINIMUM, normalised.  The measurement basis is whatever ``st``
+    holds (Circuit.py:413-418 rotates it first with MeasureX / MeasureY)."""
+    q = order[len(history)]
+    ops = {order[j]: _PROJ[h] for j, h in enumerate(history)}
+    p = []
+    for v in (0, 1):
+        o = dict(ops)
+        o[q] = _PROJ[v]
+        p.append(float(expect_ops(st, o)) + GLOBAL_MINIMUM)
+    if min(p) < 0:
+        raise RuntimeError(f'State is illegal, and your probability distribution is {p}.')
+    return p[1] / (p[0] + p[1])
+
+
 def density2prob(rho: torch.Tensor) -> np.ndarray:
     """Tools.py:242-273 with _dict=False: |rho_ii| normalised by their sum."""
     p = torch.abs(torch.diagonal(rho)).double().numpy()
