@@ -1,0 +1,67 @@
+"""The drop-in dmOperations host logic (DMNodes bookkeeping, traced qubits,
+overlaps and composite purities; MPDOSimulator/dmOperations.py) against the
+reference's own dmOperations on the same evolved states
+(tests/golden/dmops.json, made by tests/golden/make_dmops_golden.py).
+
+The engine chain behind DMNodes is replaced, in this test only, by a
+stand-in that answers its two readout calls (reduced_dm, expect_ops) from
+the oracle replaying the golden circuits' gate tensors; the GPU engine's
+own readouts are checked against the oracle in the GPU tests."""
+import json
+import os
+import sys
+
+import pytest
+import torch
+
+import golden_io as G
+from oracle import mpdo_oracle as O
+
+sys.path.insert(0, G.GOLDEN)
+from make_dmops_golden import PAIR, TRACED  # noqa: E402
+
+with open(os.path.join(G.GOLDEN, 'dmops.json')) as _f:
+    REF = json.load(_f)
+
+
+class _OracleChain:
+    """Test stand-in for the engine chain's readout calls."""
+
+    def __init__(self, st):
+        self.st, self.n = st, st.n
+
+    def reduced_dm(self, keep):
+        return O.reduced_dm(self.st, keep).numpy()
+
+    def expect_ops(self, ops):
+        return float(O.expect_ops(self.st, {q: torch.as_tensor(o) for q, o in ops.items()}))
+
+
+def _state(name):
+    info, ops, _ = G.load(name)
+    st = O.product_state([[1, 0]] * info['qn'], connected=False, dtype=G.dtype_of(info))
+    O.evolve(st, ops, chi=info['chi'], kappa=info['kappa'], max_err=info['max_truncation_err'],
+             noisy=not info['ideal'])
+    return st
+
+
+@pytest.mark.parametrize('tag', ['full', 'reduced'])
+def test_dm_operations_match_reference(tag):
+    from MPDOSimulator import dmOperations as D
+    chains = [_OracleChain(_state(name)) for name in PAIR]
+    n = chains[0].n
+
+    def nodes(ch):
+        d = D.DMNodes(ch, n, torch.complex128, 'cpu')
+        if tag == 'reduced':
+            D.reduce_dmNodes(d, reduced_index=TRACED)
+        return d
+
+    a, b = nodes(chains[0]), nodes(chains[1])
+    ref = REF[tag]
+    got = {'trace_rho': float(D.trace_rho(a)), 'trace_rho2': float(D.trace_rho2(a)),
+           'trace_rho_rho': float(D.trace_rho_rho(a, b)),
+           'trace_composited_rho': float(D.trace_composited_rho(a, b)),
+           'trace_composited_rho2': float(D.trace_composited_rho2(a, b))}
+    for k, v in ref.items():
+        assert abs(got[k] - v) < 1e-10, (k, got[k], v)
