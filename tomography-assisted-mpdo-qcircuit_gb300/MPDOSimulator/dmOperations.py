@@ -40,6 +40,12 @@ def reduce_dmNodes(qubits_nodes, conj_qubits_nodes=None, residual_index=None, re
     nodes.trace_out(reduced_index)
 
 
+def _trace_product(a: np.ndarray, b: np.ndarray) -> float:
+    """Re Tr(a b) = Re sum_ij a_ij b_ji without forming the product (O(d^2),
+    not O(d^3), for the 4096 x 4096 matrices of twelve kept qubits)."""
+    return float(np.sum(a * b.T).real)
+
+
 def trace_rho(dmNodes: DMNodes) -> Tensor:
     """dmOperations.py:40-48: Tr rho (real part)."""
     return torch.tensor(dmNodes.chain.expect_ops({}), dtype=torch.float64)
@@ -55,7 +61,7 @@ def trace_rho_rho(dmNodes_0: DMNodes, dmNodes_1: Optional[DMNodes] = None) -> Te
         raise NotImplementedError('Tr(rho rho) over more than 12 untraced qubits')
     r0 = dmNodes_0.chain.reduced_dm(keep)
     r1 = d1.chain.reduced_dm(keep)
-    return torch.tensor(np.trace(r0 @ r1).real, dtype=torch.float64)
+    return torch.tensor(_trace_product(r0, r1), dtype=torch.float64)
 
 
 def trace_rho2(dmNodes: DMNodes) -> Tensor:
@@ -74,7 +80,7 @@ def trace_composited_rho2(*dmNodes: DMNodes) -> Tensor:
     if len(keep) > 12:
         raise NotImplementedError('composite purity over more than 12 untraced qubits')
     rho = sum(d.chain.reduced_dm(keep) for d in dmNodes)
-    return torch.tensor(np.trace(rho @ rho).real / n ** 2, dtype=torch.float64)
+    return torch.tensor(_trace_product(rho, rho) / n ** 2, dtype=torch.float64)
 
 
 def expect(dmNodes: DMNodes, observables: Union[Tensor, List[Tensor]], oqs) -> List[Tensor]:
@@ -97,7 +103,7 @@ def expect(dmNodes: DMNodes, observables: Union[Tensor, List[Tensor]], oqs) -> L
         perm = [oq.index(q) for q in order] + [m + oq.index(q) for q in order]
         o = o.permute(*perm).reshape(2 ** m, 2 ** m).detach().cpu().numpy().astype(np.complex128)
         rho = dmNodes.chain.reduced_dm(order)
-        out.append(torch.tensor(np.trace(rho @ o).real, dtype=torch.float64))
+        out.append(torch.tensor(_trace_product(rho, o), dtype=torch.float64))
     return out
 
 
