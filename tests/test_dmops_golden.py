@@ -11,6 +11,7 @@ import json
 import os
 import sys
 
+import numpy as np
 import pytest
 import torch
 
@@ -65,3 +66,27 @@ def test_dm_operations_match_reference(tag):
            'trace_composited_rho2': float(D.trace_composited_rho2(a, b))}
     for k, v in ref.items():
         assert abs(got[k] - v) < 1e-10, (k, got[k], v)
+
+
+def test_cal_vector_and_reduced_dm_host_logic():
+    # TensorCircuit.cal_vector (Circuit.py:264-272) contracts the site tensors
+    # read back from the chain on the host; cal_dm(reduced_index) maps traced
+    # qubits to the kept list.  The noiseless golden circuit is pure, so the
+    # reference's rho is |psi><psi|.
+    import MPDOSimulator as S
+    info, _, dm_ref = G.load('ideal_chi_c128')
+    n = info['qn']
+
+    class Chain(_OracleChain):
+        def site(self, k):
+            return self.st.sites[k].numpy()
+
+    c = S.TensorCircuit(n, ideal=True, dtype=torch.complex128, device='cpu')
+    c._chain = Chain(_state('ideal_chi_c128'))
+    psi = c.cal_vector().numpy()[:, 0]
+    assert np.abs(np.outer(psi, psi.conj()) - dm_ref).max() < 1e-10
+    t = dm_ref.reshape([2] * (2 * n))
+    for q in (2, 0):                                   # trace qubits 2 and 0 out of the reference's rho
+        t = np.trace(t, axis1=q, axis2=q + t.ndim // 2)
+    want = t.reshape(2 ** (n - 2), 2 ** (n - 2))
+    assert np.abs(c.cal_dm([0, 2]).numpy() - want).max() < 1e-10
