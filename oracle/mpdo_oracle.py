@@ -642,9 +642,12 @@ def trace(st: MPDO) -> float:
 # ----------------------------------------------------------------------------
 # timed CPU baseline: one layer of a circuit with a time budget
 # ----------------------------------------------------------------------------
-def time_layer(st: MPDO, layer_ops, chi, kappa, max_err=None, noisy=True, budget_s: float = 20.0):
+def time_layer(st: MPDO, layer_ops, chi, kappa, max_err=None, noisy=True, budget_s: float = 20.0,
+               randomized: bool = False):
     """Run one layer (its gate sublayers and truncates) on the CPU and return
-    the estimated wall time of the whole layer.  Gate applications, QR sweeps
+    the estimated wall time of the whole layer.  ``randomized`` takes the
+    reference's randomized-SVD branch for capped SVDs of >= 10000 elements
+    (decompositions.py:112-115), as its stock code path does.  Gate applications, QR sweeps
     and kappa passes run in full; SVD right-to-left sweeps run until the budget
     is spent and the remaining steps are extrapolated from the mean measured
     step time of the same bond kind (even / odd bond).  Returns
@@ -694,7 +697,7 @@ def time_layer(st: MPDO, layer_ops, chi, kappa, max_err=None, noisy=True, budget
             l, x, aa, _ = a.shape
             _, y, cc, r = b.shape
             m = torch.einsum('lsam,mtcr->lsatcr', a, b).reshape(l * x * aa, y * cc * r)
-            u, s, vh, _ = svd_truncate(m, chi, max_err, relative=True)
+            u, s, vh, _ = svd_truncate(m, chi, max_err, relative=True, randomized=randomized)
             ss = torch.sqrt(s).to(m.dtype)
             k = s.numel()
             st.sites[idx - 1] = (u * ss[None, :]).reshape(l, x, aa, k)
@@ -705,6 +708,6 @@ def time_layer(st: MPDO, layer_ops, chi, kappa, max_err=None, noisy=True, budget
             measured_steps += 1
         if noisy:
             t0 = time.perf_counter()
-            svd_kappa(st, kappa, max_err)
+            svd_kappa(st, kappa, max_err, randomized)
             t_total += time.perf_counter() - t0
     return t_total, dict(measured_svd_steps=measured_steps, extrapolated_svd_steps=extrap_steps)
