@@ -195,7 +195,7 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU oracle --
-def cpu_layer(w, budget_s, threads=None):
+def cpu_layer(w, budget_s, threads=None, randomized=True):
     """Gates/s of the CPU oracle on a steady-state layer of the workload:
     layer 0 runs in full (bonds reach chi), layer 1 is timed with the SVD
     sweep extrapolated past the budget.  Factorisations in complex128 with the
@@ -225,10 +225,24 @@ def cpu_layer(w, budget_s, threads=None):
     st = O.product_state([[1, 0]] * w.n, connected=True, dtype=dt)
     # the reference's stock SVD: its vendored backend switches capped SVDs of
     # >= 1e4 elements to a randomized SVD (decompositions.py:112-115)
-    O.evolve(st, layers[0], chi=w.chi, kappa=w.kappa, noisy=True, randomized=True)
-    secs, info = O.time_layer(st, layers[1], w.chi, w.kappa, budget_s=budget_s, randomized=True)
+    O.evolve(st, layers[0], chi=w.chi, kappa=w.kappa, noisy=True, randomized=randomized)
+    secs, info = O.time_layer(st, layers[1], w.chi, w.kappa, budget_s=budget_s, randomized=randomized)
+    info['svd'] = ('SVDs as the reference takes them (randomized for capped matrices of >= 1e4 elements, exact '
+                   'otherwise)' if randomized else 'every SVD exact')
     gates = sum(1 for op in layers[1] if op[0] != 'truncate')
     return gates / secs, gates, secs, info, torch.get_num_threads()
+
+
+def cpu_layer_any(w, budget_s, threads=None):
+    """``cpu_layer`` with the reference's randomized branch; should that
+    branch fail on this host's LAPACK, the sample is retaken with exact SVDs
+    and says so."""
+    try:
+        return cpu_layer(w, budget_s, threads, randomized=True)
+    except Exception as e:  # noqa: BLE001 -- reported in the sample text
+        out = cpu_layer(w, budget_s, threads, randomized=False)
+        out[3]['svd'] += f' (the randomized branch failed here: {type(e).__name__}: {e})'
+        return out
 
 
 def reference_arm(args):
@@ -240,7 +254,7 @@ def reference_arm(args):
     cores = os.cpu_count() or 1
     vals = []
     for k in range(args.warmup + args.steps):
-        v, gates, secs, info, th = cpu_layer(w, args.cpu_budget / max(1, args.steps), threads=cores)
+        v, gates, secs, info, th = cpu_layer_any(w, args.cpu_budget / max(1, args.steps), threads=cores)
         if k >= args.warmup:
             vals.append(v)
         if k + 1 >= args.warmup and args.warmup > 1:
@@ -248,8 +262,7 @@ def reference_arm(args):
     # warm-up steps are cheap repeats of the same sample; the timed value is the mean
     val = sum(vals) / len(vals)
     sample = (f'steady-state layer 1 of the workload ({gates} gates) on the CPU oracle, torch {torch.__version__}, '
-              f'{th} threads, SVDs as the reference takes them (randomized for capped matrices of >= 1e4 '
-              f'elements, exact otherwise); {info["extrapolated_svd_steps"]} of '
+              f'{th} threads, {info["svd"]}; {info["extrapolated_svd_steps"]} of '
               f'{info["extrapolated_svd_steps"] + info["measured_svd_steps"]} SVD-sweep steps extrapolated')
     out = {'metric': METRIC, 'value': val, 'unit': 'gates/s', 'n_gpus': args.gpus, 'steps': args.steps,
            'warmup': args.warmup, 'ms_per_step': 1e3 * gates / val, 'higher_is_better': True, 'scaling': 'weak',
@@ -445,11 +458,10 @@ def gpu_arm(args):
            'plain': plain, 'batched_over_plain': value / plain['value']}
     print('gpu part: ' + json.dumps(out), file=sys.stderr, flush=True)
     if ws == 1 and not args.no_cpu_baseline:
-        v, gates, secs, info, th = cpu_layer(w, args.cpu_budget, threads=os.cpu_count())
+        v, gates, secs, info, th = cpu_layer_any(w, args.cpu_budget, threads=os.cpu_count())
         out['cpu_baseline'] = {'value': v, 'unit': 'gates/s', 'cores': th, 'kind': 'port',
                                'sample': f'steady-state layer 1 ({gates} gates) of the seed-0 circuit on the CPU '
-                                         f'oracle (torch CPU, randomized SVD for capped matrices of >= 1e4 '
-                                         f'elements, as the reference), {info["extrapolated_svd_steps"]} of '
+                                         f'oracle (torch CPU, {info["svd"]}), {info["extrapolated_svd_steps"]} of '
                                          f'{info["extrapolated_svd_steps"] + info["measured_svd_steps"]} SVD-sweep '
                                          f'steps extrapolated from measured ones; est. {secs:.1f} s per layer'}
     print(json.dumps(out), flush=True)
