@@ -109,8 +109,9 @@ class EngineChain:
             k = s.numel()
             ss = torch.sqrt(s).to(S.dtype)
             L, Rf = u * ss[None, :], ss[:, None] * vh
-            if k < cap and not (S.requires_grad or P.requires_grad):
+            if k < cap and max_err is None and not (S.requires_grad or P.requires_grad):
                 # zero singular values up to the cap, as the reference's pair SVD returns them
+                # (with an error rule, the rule itself drops the pair's trailing zeros)
                 L = torch.cat([L, L.new_zeros(b, cap - k)], 1)
                 Rf = torch.cat([Rf, Rf.new_zeros(cap - k, Nc)], 0)
                 k = cap

@@ -1,0 +1,110 @@
+"""Parity at the benchmarked shape: the n=32, chi=64, kappa=4 U3 + CZ/CNOT
+brickwork (seed 0) evolved by the GPU engine, against the complex128 oracle's
+readouts committed under tests/golden/ (``make_bench_parity.py``).
+
+Two forms of the workload:
+
+* as benchmarked (chi and kappa caps only).  Here the algorithm itself is
+  ill-conditioned: the chi cap keeps rounding-level singular values and the
+  split puts sqrt(S) on both factors, so rounding noise enters the sites at
+  sqrt(eps), and the kappa pass amplifies it.  The fixtures record how far
+  complex128 oracle runs that differ only in rounding (another LAPACK SVD
+  driver; a 1e-13 relative perturbation) move each readout.  The engine must
+  agree with the oracle to within 2 x that spread (1e-5 where it is smaller);
+* with the reference's relative truncation error 1e-6 (max_truncation_err),
+  which drops the rounding floor: the oracle's spread is then at the rounding
+  level and the engine must agree to 1e-5 (complex64) / 1e-8 (complex128).
+
+The errors are printed.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), 'golden')
+Z = np.array([[1, 0], [0, -1]], dtype=np.complex128)
+
+
+@pytest.fixture(scope='module')
+def mg():
+    m = pytest.importorskip('mpdo_gb300')
+    if not torch.cuda.is_available():
+        pytest.skip('needs a GPU')
+    m.build()
+    return m
+
+
+def engine_readouts(mg, depth, dtype, max_err=None):
+    """The workload through the drop-in's builders and the engine (as
+    bench.py's plain path), then the readouts the fixtures hold."""
+    from mpdo_gb300.workloads import u3_brickwork, build_circuit
+    w = u3_brickwork(n=32, depth=depth, chi=64, kappa=4, seed=0)
+    c = build_circuit(w, dtype=torch.complex64 if dtype == 'complex64' else torch.complex128, device='cuda:0')
+    ch = mg.Chain([[1, 0]] * w.n, dtype=dtype, connected=True)
+    disc = []
+    for op in c._engine_ops():
+        if op[0] == '1q':
+            ch.apply_1q(op[1], op[2])
+        elif op[0] == '2q':
+            ch.apply_2q(op[1], op[2], 2.718281828459045e-8)
+        elif op[0] == 'truncate':
+            disc.append(ch.truncate(w.chi, w.kappa, max_err, True, report=True))
+        else:
+            ch.kappa_truncate(w.kappa, max_err)
+    n = w.n
+    return {'trace': ch.expect_ops({}),
+            'z': [ch.expect_ops({q: Z}) for q in range(n)],
+            'zz': [ch.expect_ops({q: Z, q + 1: Z}) for q in range(n - 1)],
+            'marginals': [list(ch.probs([q])) for q in range(n)],
+            'rdm2': [ch.reduced_dm([q, q + 1]) for q in range(n - 1)],
+            'discarded': np.array(disc),
+            'dims': [list(map(int, d)) for d in ch.dims()]}
+
+
+def compare(got, ref):
+    r2 = [np.array([complex(*v) for v in m]).reshape(4, 4) for m in ref['rdm2']]
+    return {'trace': abs(got['trace'] - ref['trace']),
+            'z': float(np.abs(np.array(got['z']) - ref['z']).max()),
+            'zz': float(np.abs(np.array(got['zz']) - ref['zz']).max()),
+            'marginals': float(np.abs(np.array(got['marginals']) - np.array(ref['marginals'])).max()),
+            'rdm2': float(max(np.abs(a - b).max() for a, b in zip(got['rdm2'], r2)))}
+
+
+def _report(tag, err, ref):
+    print(f'\n{tag}: error vs complex128 oracle', {k: f'{v:.2e}' for k, v in err.items()},
+          '| spread of complex128 oracle runs', {k: f'{ref["conditioning"][k]:.2e}' for k in err})
+
+
+@pytest.mark.parametrize('depth,dtype', [(4, 'complex64'), (8, 'complex64'), (20, 'complex64'),
+                                         (4, 'complex128'), (8, 'complex128')])
+def test_bench_shape_against_complex128_oracle(mg, depth, dtype):
+    ref = json.load(open(os.path.join(GOLD, f'bench_n32_d{depth}.json')))
+    got = engine_readouts(mg, depth, dtype)
+    err = compare(got, ref)
+    _report(f'n=32 depth={depth} chi=64 kappa=4 {dtype}', err, ref)
+    for k, v in err.items():
+        assert v <= max(1e-5, 2 * ref['conditioning'][k]), (k, v, ref['conditioning'][k])
+    # every leg dimension of the final state as the oracle keeps it
+    assert got['dims'] == ref['dims']
+    # per-bond discarded weight of every truncate layer (the weight beyond chi
+    # is at the rounding floor here: both sides report it as ~0)
+    d_ref = np.array(ref['discarded'])
+    assert got['discarded'].shape == d_ref.shape
+    assert np.abs(got['discarded'] - d_ref).max() < 1e-6
+
+
+@pytest.mark.parametrize('dtype,tol', [('complex64', 1e-5), ('complex128', 1e-8)])
+def test_bench_shape_error_rule_strict(mg, dtype, tol):
+    # n=32, depth 20, chi=64, kappa=4 with max_truncation_err=1e-6: well conditioned
+    ref = json.load(open(os.path.join(GOLD, 'bench_n32_d20_err1e-6.json')))
+    got = engine_readouts(mg, 20, dtype, max_err=1e-6)
+    err = compare(got, ref)
+    _report(f'n=32 depth=20 chi=64 kappa=4 max_err=1e-6 {dtype}', err, ref)
+    for k, v in err.items():
+        assert v <= tol, (k, v)
+    assert got['dims'] == ref['dims']

@@ -199,8 +199,13 @@ mpdo_status mpdo_batch_run(mpdo_batch_t b, int ncirc, const mpdo_program *progs,
   };
   std::vector<std::thread> threads;
   for (int w = 1; w < W; ++w) threads.emplace_back(worker, w);
+  // worker 0 runs on the calling thread and selects the batch's device: the
+  // caller's current device is restored afterwards
+  int caller_dev = -1;
+  if (cudaGetDevice(&caller_dev) != cudaSuccess) { cudaGetLastError(); caller_dev = -1; }
   worker(0);
   for (auto &t : threads) t.join();
+  if (caller_dev >= 0) cudaSetDevice(caller_dev);
   mpdo_status first = MPDO_OK;
   for (int i = 0; i < ncirc; ++i) {
     if (status_out) status_out[i] = st[i];

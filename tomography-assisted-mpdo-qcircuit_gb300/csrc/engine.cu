@@ -33,258 +33,19 @@
 #include <unordered_map>
 #include <vector>
 
-namespace mpdo {
+#include "engine_core.cuh"
 
-// ------------------------------------------------------------ errors ----
-struct Error {
-  mpdo_status st;
-  std::string msg;
-};
-[[noreturn]] static void fail(mpdo_status s, const std::string &m) { throw Error{s, m}; }
+namespace mpdo {
 
 static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
-
-// ------------------------------------------------------------ engine ----
-struct Engine {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaStream_t own_stream = nullptr;
-  cudaMemPool_t pool = nullptr;
-  int *d_status = nullptr;
-  int status_cap = 8192;
-  int status_used = 0;
-  bool fuse_2q = true;
-  int wide_range = -1;              // verified range finder on wide bonds: 1 on, 0 off, -1 complex128 only
-  int wide_eig = -1;                // wide-bond Gram: tridiagonal eigensolver 1 on, 0 off, -1 complex128 only
-  long long wide_eig_calls = 0;
-  long long wide_range_hits = 0, wide_exact_calls = 0;
-  double wide_resid_max = 0;        // largest accepted |Y - Q Q^H Y|_F / |Y|_F
-  double wide_range_tol = 8.0;      // acceptance: residual <= tol * eps * sqrt(p) * |Y|_F
-  int max_sweeps = 60;
-  int first_status = 0;
-  // per-kernel-class profiling (CUDA events around each launch)
-  struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };
-  bool profiling = false;
-  std::vector<ProfRec> recs;
-  double acc_ms[14] = {0}, acc_flops[14] = {0}, acc_bytes[14] = {0};
-  long long acc_n[14] = {0};
-  // Freed device blocks kept for reuse, by rounded size.  Every block of an
-  // engine is used on the engine's one stream, so a block freed after its
-  // last use was enqueued can serve the next allocation at once (stream order
-  // separates the uses); the driver's allocator is then off the hot path.
-  std::unordered_map<size_t, std::vector<void *>> cache;
-  std::unordered_map<void *, size_t> live;
-  size_t cached_bytes = 0;
-};
-
-// kernel classes reported by mpdo_engine_profile_read
-enum KClass {
-  K_GEMM = 0, K_QR_FACTOR = 1, K_QR_APPLY = 2, K_JACOBI = 3, K_KRAUS1Q = 4, K_MIX2Q = 5, K_OTHER = 6,
-  K_BJACOBI = 8,  // (7 reports the wide-bond counters)
-  // phases (spans of many launches, overlapping the kernel classes)
-  P_QR_SWEEP = 9, P_SVD_SWEEP = 10, P_KAPPA = 11, P_WIDE_SVD = 12,
-  K_HETRD = 13     // cluster tridiagonalisation of wide-bond Gram matrices
-};
-constexpr int kProfClasses = 14;
-
-// Launch wrapper: when profiling, bracket the launch with events and keep the
-// algorithmic flop/byte count of the call.
-template <class F> static void prof(Engine &e, int cls, double flops, double bytes, F &&launch) {
-  if (!e.profiling) { launch(); return; }
-  Engine::ProfRec r{cls, nullptr, nullptr, flops, bytes};
-  cudaEventCreate(&r.a);
-  cudaEventCreate(&r.b);
-  cudaEventRecord(r.a, e.stream);
-  launch();
-  cudaEventRecord(r.b, e.stream);
-  e.recs.push_back(r);
-}
-static void prof_flush(Engine &e) {
-  if (e.recs.empty()) return;
-  cudaStreamSynchronize(e.stream);
-  for (auto &r : e.recs) {
-    float ms = 0;
-    cudaEventElapsedTime(&ms, r.a, r.b);
-    e.acc_ms[r.cls] += ms;
-    e.acc_flops[r.cls] += r.flops;
-    e.acc_bytes[r.cls] += r.bytes;
-    e.acc_n[r.cls] += 1;
-    cudaEventDestroy(r.a);
-    cudaEventDestroy(r.b);
-  }
-  e.recs.clear();
-}
-
-// Phase span (profiling only): events around a block of launches.
-struct Phase {
-  Engine &e;
-  Engine::ProfRec r;
-  Phase(Engine &eng, int cls) : e(eng), r{cls, nullptr, nullptr, 0, 0} {
-    if (!e.profiling) return;
-    cudaEventCreate(&r.a);
-    cudaEventCreate(&r.b);
-    cudaEventRecord(r.a, e.stream);
-  }
-  ~Phase() {
-    if (!e.profiling || !r.a) return;
-    cudaEventRecord(r.b, e.stream);
-    e.recs.push_back(r);
-  }
-};
-
-// Allocation size classes: multiples of 256 B up to 64 KiB, then eight steps
-// per power of two (at most 12.5% slack).
-static size_t size_class(size_t bytes) {
-  if (bytes <= 65536) return (bytes + 255) / 256 * 256;
-  int k = 63 - __builtin_clzll((unsigned long long)(bytes - 1));   // 2^k < bytes <= 2^(k+1)
-  const size_t step = size_t(1) << (k - 2);
-  return (bytes + step - 1) / step * step;
-}
-
-static constexpr size_t kCacheCapBytes = size_t(16) << 30;   // per engine
-
-static void release_cache(Engine &e) {
-  for (auto &kv : e.cache)
-    for (void *q : kv.second) cudaFreeAsync(q, e.stream);
-  e.cache.clear();
-  e.cached_bytes = 0;
-}
-
-static void *dalloc(Engine &e, size_t bytes) {
-  if (bytes == 0) bytes = 16;
-  const size_t sz = size_class(bytes);
-  auto it = e.cache.find(sz);
-  if (it != e.cache.end() && !it->second.empty()) {
-    void *p = it->second.back();
-    it->second.pop_back();
-    e.cached_bytes -= sz;
-    e.live[p] = sz;
-    return p;
-  }
-  void *p = nullptr;
-  cudaError_t err = cudaMallocFromPoolAsync(&p, sz, e.pool, e.stream);
-  if (err != cudaSuccess) {
-    cudaGetLastError();
-    release_cache(e);                        // give cached blocks back and retry once
-    err = cudaMallocFromPoolAsync(&p, sz, e.pool, e.stream);
-    if (err != cudaSuccess) {
-      cudaGetLastError();
-      fail(MPDO_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(err));
-    }
-  }
-  e.live[p] = sz;
-  return p;
-}
-static void dfree(Engine &e, void *p) {
-  if (!p) return;
-  auto it = e.live.find(p);
-  if (it == e.live.end()) {                  // not from dalloc: hand straight back
-    cudaFreeAsync(p, e.stream);
-    return;
-  }
-  const size_t sz = it->second;
-  e.live.erase(it);
-  e.cache[sz].push_back(p);
-  e.cached_bytes += sz;
-  if (e.cached_bytes > kCacheCapBytes) release_cache(e);
-}
-
-// Scoped device buffer
-template <typename X> struct DBuf {
-  Engine *e = nullptr;
-  X *p = nullptr;
-  size_t n = 0;
-  DBuf() = default;
-  DBuf(Engine &eng, size_t count) : e(&eng), n(count) { p = static_cast<X *>(dalloc(eng, count * sizeof(X))); }
-  DBuf(const DBuf &) = delete;
-  DBuf &operator=(const DBuf &) = delete;
-  DBuf(DBuf &&o) noexcept : e(o.e), p(o.p), n(o.n) { o.p = nullptr; }
-  DBuf &operator=(DBuf &&o) noexcept {
-    reset();
-    e = o.e; p = o.p; n = o.n; o.p = nullptr;
-    return *this;
-  }
-  X *release() { X *q = p; p = nullptr; return q; }
-  void reset() { if (p && e) dfree(*e, p); p = nullptr; }
-  ~DBuf() { if (p && e) dfree(*e, p); }
-};
-
-static int *status_slot(Engine &e, int count);
-static void check_status(Engine &e);
-
-// ------------------------------------------------------------- chain ----
-struct Site {
-  void *p = nullptr;
-  int l = 1, a = 1, r = 1;
-  size_t elems() const { return (size_t)l * 2 * a * r; }
-};
-struct Pend {
-  bool on = false;
-  std::vector<double> t;
-  int K = 1;
-  double cutoff = 0;
-};
-}  // namespace mpdo
-
-struct mpdo_engine_s {
-  mpdo::Engine e;
-};
-struct mpdo_chain_s {
-  mpdo_engine_s *eng = nullptr;
-  int n = 0;
-  int dtype = MPDO_C64;
-  std::vector<mpdo::Site> s;
-  std::vector<char> bond;
-  std::vector<mpdo::Pend> pend;
-};
-
-namespace mpdo {
-
-// ---------------------------------------------------------- helpers -----
-template <typename T> static View<T> RM(const cx<T> *p, int64_t ld, int conj = 0, int64_t bs = 0) {
-  return View<T>{p, bs, 1, ld, 0, 1, conj};
-}
-template <typename T> static View<T> CM(const cx<T> *p, int64_t ld, int conj = 0, int64_t bs = 0) {
-  return View<T>{p, bs, 1, 1, 0, ld, conj};
-}
-
-template <typename T>
-static void gemm(Engine &e, int M, int N, int K, const View<T> &A, const View<T> &B, cx<T> *C, int64_t ldc,
-                 int batch = 1, int64_t cbs = 0, cx<T> beta = czero<T>()) {
-  const double fl = 8.0 * M * N * K * batch;
-  const double by = (double)sizeof(cx<T>) * batch * ((double)M * K + (double)K * N + (double)M * N);
-  // split-K workspace for small-output long-K products
-  const int64_t tiles = (int64_t)((M + 63) / 64) * ((N + 63) / 64) * batch;
-  if (K >= 512 && tiles < 148) {
-    const int nsplit = (int)std::min<int64_t>(std::max<int64_t>(1, 296 / tiles), K / 128);
-    if (nsplit > 1) {
-      const size_t ws = (size_t)nsplit * batch * M * N;
-      DBuf<cx<T>> w(e, ws);
-      prof(e, K_GEMM, fl, by, [&] {
-        cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs, w.p, ws);
-      });
-      return;
-    }
-  }
-  prof(e, K_GEMM, fl, by, [&] { cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs); });
-}
-
-template <typename T> static cx<T> *site_ptr(mpdo_chain_s *ch, int i) { return static_cast<cx<T> *>(ch->s[i].p); }
-
-template <typename T> static void set_site(mpdo_chain_s *ch, int i, cx<T> *p, int l, int a, int r) {
-  Engine &e = ch->eng->e;
-  if (ch->s[i].p) dfree(e, ch->s[i].p);
-  ch->s[i].p = p;
-  ch->s[i].l = l; ch->s[i].a = a; ch->s[i].r = r;
-}
 
 // ---------------------------------------------------------------- QR ----
 // Householder QR of an m x n matrix (view `in`): Q (m x k, row-major, ld k),
 // R (k x n row-major), k = min(m, n).  Tall-skinny inputs go through TSQR
 // levels of shared-memory-resident chunks.
 template <typename T>
-static void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
+void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
   const size_t esz = sizeof(cx<T>);
   const size_t cap = 200 * 1024;
   struct Level {
@@ -361,7 +122,7 @@ static void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
 // R factors of a batch of equally shaped m x n matrices (input b at in.bs*b):
 // R (batch x k x n, row-major, k = min(m, n)), by the same TSQR levels as qr().
 template <typename T>
-static void qr_r_batched(Engine &e, int batch, int m, int n, const View<T> &in, cx<T> *R) {
+void qr_r_batched(Engine &e, int batch, int m, int n, const View<T> &in, cx<T> *R) {
   const size_t esz = sizeof(cx<T>);
   const size_t cap = 200 * 1024;
   DBuf<cx<T>> v, tau, rs, rs_prev;
@@ -400,7 +161,7 @@ static void qr_r_batched(Engine &e, int batch, int m, int n, const View<T> &in, 
 }
 
 template <typename T>
-static void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W, DBuf<T> &sigma) {
+void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W, DBuf<T> &sigma) {
   const int k = std::min(m, n);
   DBuf<cx<T>> R(e, (size_t)k * n);
   qr<T>(e, m, n, in, nullptr, R.p);
@@ -706,7 +467,7 @@ static void svd_split(Engine &e, const cx<T> *Y, int Mr, int Nc, KeepFn keep_fn,
 // reference decomposes a matrix with nsv singular values; entries beyond the
 // computed spectrum are zero.
 template <typename T>
-static int error_rule_keep(const std::vector<T> &s_in, int nsv, int max_sv, double err, bool relative) {
+int error_rule_keep(const std::vector<T> &s_in, int nsv, int max_sv, double err, bool relative) {
   int n_err = max_sv;
   if (err >= 0 && nsv > 0) {
     std::vector<T> te(nsv);
@@ -731,7 +492,7 @@ template <typename T> static void materialize_touching(mpdo_chain_s *ch, int sit
   if (site - 1 >= 0 && ch->pend[site - 1].on) materialize_pair<T>(ch, site - 1);
   if (site < ch->n - 1 && ch->pend[site].on) materialize_pair<T>(ch, site);
 }
-template <typename T> static void materialize_all(mpdo_chain_s *ch) {
+template <typename T> void materialize_all(mpdo_chain_s *ch) {
   for (int i = 0; i + 1 < ch->n; ++i)
     if (ch->pend[i].on) materialize_pair<T>(ch, i);
 }
@@ -962,7 +723,7 @@ template <typename T> static void kappa_pass(mpdo_chain_s *ch, int kappa, double
   }
 }
 
-static bool connected(mpdo_chain_s *ch) {
+bool connected(mpdo_chain_s *ch) {
   for (int i = 0; i + 1 < ch->n; ++i)
     if (!ch->bond[i]) return false;
   return true;
@@ -1223,13 +984,13 @@ static void sample_chain(mpdo_chain_s *ch, const int *order, int L, int64_t shot
 }
 
 // ------------------------------------------------------------ status ----
-static int *status_slot(Engine &e, int count) {
+int *status_slot(Engine &e, int count) {
   if (e.status_used + count > e.status_cap) check_status(e);
   int *p = e.d_status + e.status_used;
   e.status_used += count;
   return p;
 }
-static void check_status(Engine &e) {
+void check_status(Engine &e) {
   if (e.status_used == 0) return;
   std::vector<int> h(e.status_used);
   MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), e.d_status, h.size() * sizeof(int), cudaMemcpyDeviceToHost, e.stream));
@@ -1240,27 +1001,20 @@ static void check_status(Engine &e) {
   e.status_used = 0;
 }
 
+// instantiations of the factorisation steps shared with the adjoint
+#define MPDO_INST_CORE(T)                                                                                 \
+  template void qr<T>(Engine &, int, int, const View<T> &, cx<T> *, cx<T> *);                            \
+  template void qr_r_batched<T>(Engine &, int, int, int, const View<T> &, cx<T> *);                      \
+  template void right_svd<T>(Engine &, int, int, const View<T> &, DBuf<cx<T>> &, DBuf<T> &);            \
+  template int error_rule_keep<T>(const std::vector<T> &, int, int, double, bool);                       \
+  template void materialize_all<T>(mpdo_chain_s *);
+MPDO_INST_CORE(float)
+MPDO_INST_CORE(double)
+
 }  // namespace mpdo
 
 // ================================================================ C ABI ====
 using namespace mpdo;
-
-template <typename F> static mpdo_status guard(F &&f) {
-  try {
-    f();
-    return MPDO_OK;
-  } catch (const Error &err) {
-    g_last_error = err.msg;
-    return err.st;
-  } catch (const CudaError &ce) {
-    g_last_error = std::string(ce.expr) + ": " + cudaGetErrorString(ce.err) + " (" + ce.file + ":" +
-                   std::to_string(ce.line) + ")";
-    return MPDO_ERR_CUDA;
-  } catch (const std::exception &ex) {
-    g_last_error = ex.what();
-    return MPDO_ERR_INVALID;
-  }
-}
 
 #define DISPATCH(ch, FN, ...)                        \
   do {                                               \

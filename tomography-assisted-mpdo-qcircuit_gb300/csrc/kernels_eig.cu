@@ -311,10 +311,21 @@ cudaError_t hetrd_cluster(cudaStream_t st, int n, const cx<T> *G, T *d, T *e, cx
   const int csz = (n + EIG_NC - 1) / EIG_NC;
   const size_t bytes = ((size_t)n * EIG_NC + 3 * (size_t)n) * sizeof(cx<T>);
   smem_optin(k_hetrd<T>);
-  static std::once_flag nonportable;
-  std::call_once(nonportable, [] {
-    cudaFuncSetAttribute(k_hetrd<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  });
+  // cluster sizes above 8 need the non-portable opt-in, which CUDA keeps per
+  // device: set once per (kernel, device), like the shared-memory ceiling
+  {
+    static std::mutex mu;
+    static std::set<int> done;
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!done.count(dev)) {
+      err = cudaFuncSetAttribute(k_hetrd<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if (err != cudaSuccess) return err;
+      done.insert(dev);
+    }
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(csz, 1, 1);
   cfg.blockDim = dim3(EIG_NT, 1, 1);

@@ -69,8 +69,11 @@ struct Level {
   cx<float> *v, *tau, *rs;
 };
 
-// The TSQR plan of the engine (chunks that fit shared memory, compact R
-// stacking), laid out in the scratch array.  Returns the bytes needed.
+// A TSQR plan in the engine's style (row chunks that fit shared memory,
+// compact R stacking), laid out in the scratch array.  Its chunks are sized
+// for (n + 1) columns of shared memory where the engine's qr() reserves
+// (n + 2), so for tall inputs the chunking -- and with it the rounding -- can
+// differ slightly from mpdo_debug_svd.  Returns the bytes needed.
 size_t plan(int m, int n, unsigned char *base, Level *lv, int *nlev, cx<float> **U, cx<float> **xws,
             cx<float> **wws, int **status) {
   const size_t esz = sizeof(cx<float>);
