@@ -219,6 +219,24 @@ mpdo_status mpdo_batch_run(mpdo_batch_t b, int ncirc, const mpdo_program *progs,
                            int *worker_out, int *status_out);
 const char *mpdo_batch_error(mpdo_batch_t b, int circuit);
 
+/* ---- Reverse-mode gradient ------------------------------------------------
+ * No counterpart in the reference (its gate tensors detach the angles,
+ * SingleGates.py:181-185, YGates.py:66-68); it differentiates the evolution
+ * the reference defines (Circuit.py:469-491, TNNOptimizer.py:87-197).
+ * Evolves `prog` (connected = 1, max_err < 0; z / zz / discarded ignored),
+ * evaluates loss = Re Tr(rho H) for a Hermitian H given as a matrix-product
+ * operator and writes dloss/d(every gate tensor) into grad_out, laid out like
+ * prog->kraus (interleaved complex, cotangent = dL/dRe + i dL/dIm).
+ * mpo_dims: n + 1 bond dimensions D_0 = 1 .. D_n = 1 (each <= 64); mpo: per
+ * site k, W_k[D_k][D_k+1][out][in] complex, concatenated.  Every split keeps
+ * at most the numerical rank (singular values above rank_tol * s_0) and
+ * pending 2q gates are materialised by QR (no absolute cutoff); the
+ * 1/(lam_j - lam_i) terms of the split adjoints are broadened to
+ * d / (d^2 + (broadening lam_0)^2).  The chain is checkpointed per truncate
+ * segment and each segment is recomputed once in the reverse sweep. */
+mpdo_status mpdo_program_grad(mpdo_engine_t eng, const mpdo_program *prog, const int *mpo_dims, const double *mpo,
+                              double rank_tol, double broadening, double *loss_out, double *grad_out);
+
 /* Kernel-level test hooks (no counterpart in the reference).  Host in/out,
  * row-major complex (interleaved doubles).
  * mpdo_debug_qr:  A (m x n) = Q (m x k) R (k x n), k = min(m, n), Householder

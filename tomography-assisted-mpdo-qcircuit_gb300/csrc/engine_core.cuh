@@ -232,7 +232,7 @@ template <typename T> inline View<T> CM(const cx<T> *p, int64_t ld, int conj = 0
 
 template <typename T>
 inline void gemm(Engine &e, int M, int N, int K, const View<T> &A, const View<T> &B, cx<T> *C, int64_t ldc,
-                 int batch = 1, int64_t cbs = 0, cx<T> beta = czero<T>()) {
+                 int batch = 1, int64_t cbs = 0, cx<T> beta = czero<T>(), cx<T> alpha = cmk<T>(T(1), T(0))) {
   const double fl = 8.0 * M * N * K * batch;
   const double by = (double)sizeof(cx<T>) * batch * ((double)M * K + (double)K * N + (double)M * N);
   // split-K workspace for small-output long-K products
@@ -243,12 +243,12 @@ inline void gemm(Engine &e, int M, int N, int K, const View<T> &A, const View<T>
       const size_t ws = (size_t)nsplit * batch * M * N;
       DBuf<cx<T>> w(e, ws);
       prof(e, K_GEMM, fl, by, [&] {
-        cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs, w.p, ws);
+        cgemm<T>(e.stream, M, N, K, batch, alpha, A, B, beta, C, ldc, 1, cbs, w.p, ws);
       });
       return;
     }
   }
-  prof(e, K_GEMM, fl, by, [&] { cgemm<T>(e.stream, M, N, K, batch, cmk<T>(T(1), T(0)), A, B, beta, C, ldc, 1, cbs); });
+  prof(e, K_GEMM, fl, by, [&] { cgemm<T>(e.stream, M, N, K, batch, alpha, A, B, beta, C, ldc, 1, cbs); });
 }
 
 template <typename T> inline cx<T> *site_ptr(mpdo_chain_s *ch, int i) { return static_cast<cx<T> *>(ch->s[i].p); }

@@ -141,6 +141,47 @@ void env_dot(cudaStream_t st, const cx<T> *E, const cx<T> *R, int64_t msize, int
 template <typename T>
 void gather_mats(cudaStream_t st, const cx<T> *src, cx<T> *dst, const int *idx, int64_t msize, int batch);
 
+// ------------------------------------------------- adjoint (kernels_adj.cu) --
+// Cotangent convention: Xbar = dL/dRe X + i dL/dIm X for a real loss L.
+// Abar[l][s][a][r] = sum_{x,k} conj(G[x][s][k]) Obar[l][x][aK+k][r]
+template <typename T>
+void kraus1q_bwd(cudaStream_t st, const cx<T> *Ob, cx<T> *Ab, int L, int Aa, int R, const double *g_host, int K);
+// acc[(x*2+s)*K + k] += sum_{l,a,r} Obar[l][x][aK+k][r] conj(A[l][s][a][r])   (double accumulators)
+template <typename T>
+void kraus1q_grad(cudaStream_t st, const cx<T> *Ob, const cx<T> *A, int L, int Aa, int R, int K, double2 *acc);
+// Wbar[s][k][t][c][r] = sum_{x,y,q} conj(Tg[x][y][s][t][q]) Zbar[x][k][y][cK+q][r]
+template <typename T>
+void mix2q_bwd(cudaStream_t st, const cx<T> *Zb, cx<T> *Wb, int kr, int Cc, int R, const double *t_host, int K);
+// acc[(((x*2+y)*2+s)*2+t)*K + q] += sum_{k,c,r} Zbar[x][k][y][cK+q][r] conj(W[s][k][t][c][r])
+template <typename T>
+void mix2q_grad(cudaStream_t st, const cx<T> *Zb, const cx<T> *W, int kr, int Cc, int R, int K, double2 *acc);
+// B (m x k, ld ldb) <- B R^-H, R upper triangular k x k (ld ldr); rank-deficient columns give zeros
+template <typename T>
+void trsm_rh(cudaStream_t st, cx<T> *B, int m, int k, int64_t ldb, const cx<T> *R, int64_t ldr);
+// M (n x n) <- lower triangle mirrored to the upper one, real diagonal
+template <typename T>
+void copyltu(cudaStream_t st, cx<T> *M, int n);
+// truncated-split adjoint coefficients (b x k) from U^H Ubar_k, s and the L / R dot products
+template <typename T>
+void split_K(cudaStream_t st, const cx<T> *UhUb, const T *s, int b, int k, const double *dl, const double *dr,
+             double beta, cx<T> *Kout);
+// kappa-pass adjoint coefficients (a x k): F o (V^H X) on discarded rows, zero on the kept block
+template <typename T>
+void kappa_C(cudaStream_t st, const cx<T> *VhX, const T *s, int a, int k, double beta, cx<T> *C);
+// out[j] = Re sum_i conj(A[i si + j sj]) B[i si + j sj]
+template <typename T>
+void redot(cudaStream_t st, const cx<T> *A, const cx<T> *B, int n, int64_t len, int64_t si, int64_t sj, double *out);
+// adjoint of blockdiag2: Qbar[(b a)][k] = sum_x Sbar[b][x][a][x kq + k]
+template <typename T>
+void blockdiag2_bwd(cudaStream_t st, const cx<T> *Sb, cx<T> *Qb, int B, int Aa, int kq);
+// out[o][l][x][rest] = sum_{i, y} W[i wi + o wo + 2x + y] in[i][l][y][rest]  (MPO environment mix)
+template <typename T>
+void mpo_mix(cudaStream_t st, const cx<T> *in, cx<T> *out, const cx<T> *W, int Din, int Dout, int64_t wi, int64_t wo,
+             int64_t L, int64_t rest);
+// y += alpha x
+template <typename T>
+void axpy(cudaStream_t st, cx<T> *y, const cx<T> *x, int64_t n, double alpha);
+
 // Message returned by mpdo_last_error() on the calling thread.
 void set_last_error(const std::string &msg);
 
