@@ -233,9 +233,12 @@ const char *mpdo_batch_error(mpdo_batch_t b, int circuit);
  * pending 2q gates are materialised by QR (no absolute cutoff); the
  * 1/(lam_j - lam_i) terms of the split adjoints are broadened to
  * d / (d^2 + (broadening lam_0)^2).  The chain is checkpointed per truncate
- * segment and each segment is recomputed once in the reverse sweep. */
+ * segment and each segment is recomputed once in the reverse sweep.
+ * phase_ms (nullable, 3 doubles): CUDA-event spans of the forward pass, the
+ * readout with its adjoint, and the reverse sweep. */
 mpdo_status mpdo_program_grad(mpdo_engine_t eng, const mpdo_program *prog, const int *mpo_dims, const double *mpo,
-                              double rank_tol, double broadening, double *loss_out, double *grad_out);
+                              double rank_tol, double broadening, double *loss_out, double *grad_out,
+                              double *phase_ms);
 
 /* Kernel-level test hooks (no counterpart in the reference).  Host in/out,
  * row-major complex (interleaved doubles).

@@ -91,11 +91,12 @@ def test_bench_shape_against_complex128_oracle(mg, depth, dtype):
         assert v <= max(1e-5, 2 * ref['conditioning'][k]), (k, v, ref['conditioning'][k])
     # every leg dimension of the final state as the oracle keeps it
     assert got['dims'] == ref['dims']
-    # per-bond discarded weight of every truncate layer (the weight beyond chi
-    # is at the rounding floor here: both sides report it as ~0)
+    # per-bond discarded weight of every truncate layer: the weight beyond chi
+    # is below 1e-8 here; complex64 resolves it to the rounding of
+    # 1 - kept / total in single precision
     d_ref = np.array(ref['discarded'])
     assert got['discarded'].shape == d_ref.shape
-    assert np.abs(got['discarded'] - d_ref).max() < 1e-6
+    assert np.abs(got['discarded'] - d_ref).max() < (2e-5 if dtype == 'complex64' else 1e-9)
 
 
 @pytest.mark.parametrize('dtype,tol', [('complex64', 1e-5), ('complex128', 1e-8)])

@@ -608,7 +608,7 @@ template <typename T> void free_chain(Engine &e, mpdo_chain_s *ch) {
 
 template <typename T>
 void program_grad(mpdo_engine_s *eng, const mpdo_program *prog, const int *Dd, const double *mpo, double rank_tol,
-                  double beta, double *loss_out, double *grad_out) {
+                  double beta, double *loss_out, double *grad_out, double *phase_ms) {
   Engine &e = eng->e;
   const int n = prog->n;
   if (!prog->connected) fail(MPDO_ERR_INVALID, "the adjoint needs a connected chain (connected = 1)");
@@ -660,6 +660,10 @@ void program_grad(mpdo_engine_s *eng, const mpdo_program *prog, const int *Dd, c
   const int nseg = (int)seg_end.size();
   std::vector<mpdo_chain_s> ckpt(nseg);
   std::vector<std::vector<int>> ck_pend(nseg);
+  // phase events: forward (with checkpoints), readout and its adjoint, reverse sweep
+  cudaEvent_t ev[4];
+  for (auto &x : ev) MPDO_CUDA_CHECK(cudaEventCreate(&x));
+  MPDO_CUDA_CHECK(cudaEventRecord(ev[0], e.stream));
   // forward with checkpoints
   c.record = false;
   for (int sgi = 0; sgi < nseg; ++sgi) {
@@ -668,8 +672,10 @@ void program_grad(mpdo_engine_s *eng, const mpdo_program *prog, const int *Dd, c
     ck_pend[sgi] = c.pend_op;
     run_ops<T>(c, sgi ? seg_end[sgi - 1] : 0, seg_end[sgi], sgi == nseg - 1);
   }
+  MPDO_CUDA_CHECK(cudaEventRecord(ev[1], e.stream));
   Cot<T> g;
   *loss_out = mpo_loss_grad<T>(c, Dd, Wd.p, woff, g);
+  MPDO_CUDA_CHECK(cudaEventRecord(ev[2], e.stream));
   // reverse sweep, one segment at a time
   for (int sgi = nseg - 1; sgi >= 0; --sgi) {
     clone_into<T>(e, &chain, &ckpt[sgi]);
@@ -684,8 +690,16 @@ void program_grad(mpdo_engine_s *eng, const mpdo_program *prog, const int *Dd, c
     backprop<T>(c, g);
   }
   free_chain<T>(e, &chain);
+  MPDO_CUDA_CHECK(cudaEventRecord(ev[3], e.stream));
   check_status(e);
   MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  if (phase_ms)
+    for (int q = 0; q < 3; ++q) {
+      float ms = 0;
+      MPDO_CUDA_CHECK(cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
+      phase_ms[q] = ms;
+    }
+  for (auto &x : ev) cudaEventDestroy(x);
   if (e.first_status) {
     const int fs = e.first_status;
     e.first_status = 0;
@@ -708,7 +722,7 @@ using namespace mpdo;
 
 extern "C" mpdo_status mpdo_program_grad(mpdo_engine_t eng, const mpdo_program *prog, const int *mpo_dims,
                                          const double *mpo, double rank_tol, double broadening, double *loss_out,
-                                         double *grad_out) {
+                                         double *grad_out, double *phase_ms) {
   return guard([&] {
     if (!eng || !prog || !mpo_dims || !mpo || !loss_out || !grad_out) fail(MPDO_ERR_INVALID, "NULL argument");
     if (prog->n < 2) fail(MPDO_ERR_INVALID, "n must be >= 2");
@@ -716,8 +730,8 @@ extern "C" mpdo_status mpdo_program_grad(mpdo_engine_t eng, const mpdo_program *
     if (!(broadening >= 0)) fail(MPDO_ERR_INVALID, "broadening must be >= 0");
     MPDO_CUDA_CHECK(cudaSetDevice(eng->e.device));
     if (prog->dtype == MPDO_C64)
-      program_grad<float>(eng, prog, mpo_dims, mpo, rank_tol, broadening, loss_out, grad_out);
+      program_grad<float>(eng, prog, mpo_dims, mpo, rank_tol, broadening, loss_out, grad_out, phase_ms);
     else
-      program_grad<double>(eng, prog, mpo_dims, mpo, rank_tol, broadening, loss_out, grad_out);
+      program_grad<double>(eng, prog, mpo_dims, mpo, rank_tol, broadening, loss_out, grad_out, phase_ms);
   });
 }

@@ -468,17 +468,19 @@ static void svd_split(Engine &e, const cx<T> *Y, int Mr, int Nc, KeepFn keep_fn,
 // computed spectrum are zero.
 template <typename T>
 int error_rule_keep(const std::vector<T> &s_in, int nsv, int max_sv, double err, bool relative) {
+  // evaluated in double whatever T: in single precision the cumulative
+  // norms' rounding (~6e-8 s_0) is a tenth of a 1e-6 relative threshold
   int n_err = max_sv;
   if (err >= 0 && nsv > 0) {
-    std::vector<T> te(nsv);
-    T acc = T(0);
+    std::vector<double> te(nsv);
+    double acc = 0.0;
     for (int i = 0; i < nsv; ++i) {
-      const T v = i < (int)s_in.size() ? s_in[i] : T(0);
+      const double v = i < (int)s_in.size() ? (double)s_in[i] : 0.0;
       acc += v * v;
       te[i] = std::sqrt(acc);
     }
-    const T s0 = s_in.empty() ? T(0) : s_in[0];
-    const T thr = relative ? (T)err * s0 : (T)err;
+    const double s0 = s_in.empty() ? 0.0 : (double)s_in[0];
+    const double thr = relative ? err * s0 : err;
     for (int idx = 0; idx < nsv - 1; ++idx)
       if (te[nsv - 1] - te[idx] <= thr) { n_err = idx + 1; break; }
   }

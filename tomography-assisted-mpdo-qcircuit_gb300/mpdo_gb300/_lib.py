@@ -81,7 +81,7 @@ SIGNATURES = {
     'mpdo_batch_engine': (_I, [_P, _I, C.POINTER(_P)]),
     'mpdo_batch_run': (_I, [_P, _I, C.POINTER(Program), C.POINTER(_P), _IP, _IP]),
     'mpdo_batch_error': (C.c_char_p, [_P, _I]),
-    'mpdo_program_grad': (_I, [_P, C.POINTER(Program), _IP, _DP, _D, _D, _DP, _DP]),
+    'mpdo_program_grad': (_I, [_P, C.POINTER(Program), _IP, _DP, _D, _D, _DP, _DP, _DP]),
 }
 
 _lock = threading.Lock()

@@ -110,10 +110,12 @@ def _flatten(ops) -> tuple:
 
 def program_grad(ops, n: int, terms, chi: Optional[int], kappa: Optional[int], dtype: str = 'complex64',
                  noisy: bool = True, vectors=None, rank_tol: Optional[float] = None,
-                 broadening: Optional[float] = None, engine: Optional[Engine] = None):
+                 broadening: Optional[float] = None, engine: Optional[Engine] = None, timing: Optional[dict] = None):
     """Loss and its gradient with respect to every op's Kraus tensor (a list
     aligned with ``ops``: complex128 arrays shaped like the op's tensor, None
-    for truncate / kappa ops), in torch's convention dL/dRe + i dL/dIm."""
+    for truncate / kappa ops), in torch's convention dL/dRe + i dL/dIm.
+    ``timing`` (a dict) receives the CUDA-event spans of the forward pass,
+    the readout with its adjoint and the reverse sweep, in ms."""
     dtype = 'complex128' if str(dtype).endswith('128') else 'complex64'
     eng = engine or Engine.get(0)
     lib = eng._lib
@@ -136,10 +138,13 @@ def program_grad(ops, n: int, terms, chi: Optional[int], kappa: Optional[int], d
     wbuf = _cplx(W)
     grad = np.zeros_like(flat)
     loss = C.c_double()
+    ph = np.zeros(3)
     check(lib.mpdo_program_grad(eng.handle, C.byref(pr), dims.ctypes.data_as(C.POINTER(C.c_int)), _dptr(wbuf),
                                 float(rank_tol if rank_tol is not None else DEFAULT_RANK_TOL[dtype]),
                                 float(broadening if broadening is not None else DEFAULT_BROADENING[dtype]),
-                                C.byref(loss), _dptr(grad)))
+                                C.byref(loss), _dptr(grad), _dptr(ph)))
+    if timing is not None:
+        timing.update(forward_ms=float(ph[0]), readout_ms=float(ph[1]), reverse_ms=float(ph[2]))
     grads = []
     for j, t in enumerate(tens):
         if t is None:
