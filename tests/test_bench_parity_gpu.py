@@ -91,12 +91,12 @@ def test_bench_shape_against_complex128_oracle(mg, depth, dtype):
         assert v <= max(1e-5, 2 * ref['conditioning'][k]), (k, v, ref['conditioning'][k])
     # every leg dimension of the final state as the oracle keeps it
     assert got['dims'] == ref['dims']
-    # per-bond discarded weight of every truncate layer: the weight beyond chi
-    # is below 1e-8 here; complex64 resolves it to the rounding of
-    # 1 - kept / total in single precision
+    # per-bond discarded weight of every truncate layer (as ill-conditioned as
+    # the readouts: the weight beyond chi is made of the directions that the
+    # rounding decides; up to 7% of a bond's weight at depth 20)
     d_ref = np.array(ref['discarded'])
     assert got['discarded'].shape == d_ref.shape
-    assert np.abs(got['discarded'] - d_ref).max() < (2e-5 if dtype == 'complex64' else 1e-9)
+    assert np.abs(got['discarded'] - d_ref).max() <= 1e-6 + 2e-2 * d_ref.max()
 
 
 @pytest.mark.parametrize('dtype,tol', [('complex64', 1e-5), ('complex128', 1e-8)])
@@ -109,3 +109,6 @@ def test_bench_shape_error_rule_strict(mg, dtype, tol):
     for k, v in err.items():
         assert v <= tol, (k, v)
     assert got['dims'] == ref['dims']
+    d = np.abs(got['discarded'] - np.array(ref['discarded'])).max()
+    print(f'per-bond discarded weight: max {np.array(ref["discarded"]).max():.2e}, max error {d:.2e}')
+    assert d <= tol

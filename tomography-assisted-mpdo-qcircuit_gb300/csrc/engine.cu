@@ -434,7 +434,14 @@ static void svd_split(Engine &e, const cx<T> *Y, int Mr, int Nc, KeepFn keep_fn,
   int keep = keep_fn(sg.p, nsv_ref);
   if (std::min(keep, nsv_ref) > kr) fail(MPDO_ERR_BAD_SHAPE, "internal: kept more vectors than refined");
   keep_out = keep;
-  if (wsum) sigma_weights<T>(e.stream, sg.p, Mr, keep, wsum);
+  if (wsum) {
+    // kept weight from the (refined) kept singular values; the total from
+    // |Y|_F^2 accumulated in double, so that total - kept does not depend on
+    // how accurately the discarded values themselves were computed (the wide
+    // path only estimates them from the Gram matrix)
+    sigma_weights<T>(e.stream, sg.p, Mr, keep, wsum);
+    sumsq<T>(e.stream, Y, (size_t)Mr * Nc, wsum + 1);
+  }
   const int kk = std::min(keep, nsv_ref);
   (void)kr;
   Lout = DBuf<cx<T>>(e, (size_t)Mr * std::max(keep, 1));

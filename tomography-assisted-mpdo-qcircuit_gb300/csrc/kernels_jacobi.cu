@@ -201,8 +201,16 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
     cx<T> *uo = uout + (int64_t)b * m * n + (int64_t)rank * m;
     for (int i = lane; i < m; i += 32) uo[i] = cscale<T>(X[(int64_t)j * m + i], inv);
     if (wantW) {
+      // the accumulated rotations leave each column's norm off 1 by the
+      // rounding of every rotation applied to it (in single precision a
+      // bias of ~2e-7 per kappa pass that the site norms would inherit):
+      // the columns are written unit-normalised
+      T wn = T(0);
+      for (int i = lane; i < n; i += 32) wn += cabs2<T>(W[(int64_t)j * n + i]);
+      wn = wsum(wn);
+      const T winv = wn > T(0) ? T(1) / sqrt(wn) : T(0);
       cx<T> *wo = wout + (int64_t)b * n * n + (int64_t)rank * n;
-      for (int i = lane; i < n; i += 32) wo[i] = W[(int64_t)j * n + i];
+      for (int i = lane; i < n; i += 32) wo[i] = cscale<T>(W[(int64_t)j * n + i], winv);
     }
     if (lane == 0) {
       sigma[(int64_t)b * n + rank] = sj;
