@@ -81,8 +81,11 @@ mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
  *   "wide_eig"   the exact wide-bond path diagonalises the Gram matrix by
  *                Householder tridiagonalisation on a thread-block cluster +
  *                bisection / inverse iteration (1), or by block Jacobi (0);
- *                -1 (default): tridiagonal for complex128 only (in
- *                complex64 it is less accurate than Jacobi on graded Grams).
+ *                -1 (default): tridiagonal for complex128, block Jacobi for
+ *                complex64.  Both are followed by a Rayleigh-Ritz refinement
+ *                in the leading (want + wide_oversample) directions.
+ *   "wide_oversample" extra Rayleigh-Ritz directions of a wide bond beyond
+ *                the kept count (default 16).
  *   "max_sweeps" Jacobi sweep limit (default 60). */
 mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double value);
 /* Wait for all queued work; returns the first deferred device status

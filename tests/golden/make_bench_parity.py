@@ -37,6 +37,12 @@ can agree with another one more closely than this spread.  With an error
 rule that drops the rounding floor (``--max-err 1e-6``) the spread falls to
 the rounding level.
 
+``--fp32-storage`` records, beside it, how far the same evolution moves when
+the state is stored in complex64 (every factorisation still in complex128,
+as the oracle does for complex64 inputs): the floor that rounding the
+state to single precision after every operation sets for any complex64
+implementation.
+
     python tests/golden/make_bench_parity.py --depth 20 --conditioning 2 --out tests/golden/bench_n32_d20.json
 """
 from __future__ import annotations
@@ -109,7 +115,7 @@ def _svd_gesvd(M):
     return torch.from_numpy(u), torch.from_numpy(s), torch.from_numpy(vh)
 
 
-def evolve(w, ops, max_err, perturb=0.0, pseed=1, driver=None, log=True):
+def evolve(w, ops, max_err, perturb=0.0, pseed=1, driver=None, log=True, dtype=torch.complex128):
     """engine_path's evolution, recording every SVD-sweep step's discarded
     weight sum(s_rest^2) / sum(s^2) (bonds n-2 .. 0 run right to left)."""
     disc_steps, discarded = [], []
@@ -124,8 +130,10 @@ def evolve(w, ops, max_err, perturb=0.0, pseed=1, driver=None, log=True):
     if driver == 'gesvd':
         O._svd128 = _svd_gesvd
     gen = torch.Generator().manual_seed(pseed)
-    st = O.product_state([[1, 0]] * w.n, connected=True)
+    st = O.product_state([[1, 0]] * w.n, connected=True, dtype=dtype)
     ch = EP.EngineChain(st)
+    if dtype != torch.complex128:
+        ops = [(o[0],) + tuple(x.to(dtype) if torch.is_tensor(x) else x for x in o[1:]) for o in ops]
     t0, li = time.time(), 0
     try:
         for op in ops:
@@ -151,6 +159,7 @@ def evolve(w, ops, max_err, perturb=0.0, pseed=1, driver=None, log=True):
         ch.materialize_all()
     finally:
         O.svd_truncate, O._svd128 = orig_trunc, orig_svd
+    st.sites = [x.to(torch.complex128) for x in st.sites]
     res = readouts(st)
     res.update({'discarded': discarded, 'dims': [list(s.shape) for s in st.sites]})
     return res
@@ -165,6 +174,7 @@ def main():
     ap.add_argument('--seed', type=int, default=0)
     ap.add_argument('--max-err', type=float, default=None)
     ap.add_argument('--conditioning', type=int, default=0, help='perturbation seeds (plus one gesvd run)')
+    ap.add_argument('--fp32-storage', action='store_true')
     ap.add_argument('--threads', type=int, default=0)
     ap.add_argument('--out', required=True)
     a = ap.parse_args()
@@ -185,6 +195,11 @@ def main():
                 cond[k] = max(cond.get(k, 0.0), v)
             print(name, {k: f'{v:.2e}' for k, v in d.items()}, flush=True)
         res['conditioning'] = cond
+    if a.fp32_storage:
+        d = diff(res, evolve(w, ops, a.max_err, dtype=torch.complex64))
+        d['how'] = 'state stored in complex64 after every operation, factorisations in complex128'
+        res['fp32_storage'] = d
+        print('fp32 storage', {k: (f'{v:.2e}' if isinstance(v, float) else v) for k, v in d.items()}, flush=True)
     res.update({'workload': w.name, 'n': w.n, 'depth': w.depth, 'chi': w.chi, 'kappa': w.kappa, 'seed': a.seed,
                 'max_err': a.max_err, 'noise': w.noise,
                 'oracle': 'oracle.engine_path, complex128, exact SVDs (LAPACK)', 'torch': torch.__version__})

@@ -23,7 +23,8 @@ FILES = ('ideal_cz.mat', 'czDefault.mat')
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE', '/root/reference'))
+    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE'), required='MPDO_REFERENCE' not in os.environ,
+                    help='root of the reference checkout (or set MPDO_REFERENCE)')
     args = ap.parse_args()
     _install(args.reference)
     from MPDOSimulator import RealNoise as R

@@ -73,7 +73,8 @@ def _capture_ops(c, gate_nodes):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE', '/root/reference'))
+    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE'), required='MPDO_REFERENCE' not in os.environ,
+                    help='root of the reference checkout (or set MPDO_REFERENCE)')
     ap.add_argument('--out', default=HERE)
     ap.add_argument('--only', default='', help='comma-separated case names (default: all)')
     args = ap.parse_args()

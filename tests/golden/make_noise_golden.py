@@ -23,7 +23,8 @@ ATTRS = ('decayTensor', 'dephasingTensor', 'dpCTensor', 'dpCTensor2', 'apdeCTens
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE', '/root/reference'))
+    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE'), required='MPDO_REFERENCE' not in os.environ,
+                    help='root of the reference checkout (or set MPDO_REFERENCE)')
     args = ap.parse_args()
     _install(args.reference)
     from MPDOSimulator.NoiseChannel import NoiseChannel

@@ -28,7 +28,8 @@ def orientations(n):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE', '/root/reference'))
+    ap.add_argument('--reference', default=os.environ.get('MPDO_REFERENCE'), required='MPDO_REFERENCE' not in os.environ,
+                    help='root of the reference checkout (or set MPDO_REFERENCE)')
     args = ap.parse_args()
     _install(args.reference)
     import MPDOSimulator as S

@@ -133,4 +133,28 @@ def test_brickwork_kraus_gradients_match_oracle_autograd(AD):
             continue
         worst = max(worst, float(np.abs(g.reshape(leaf.shape) - leaf.grad.numpy()).max()))
     print(f'\nbrickwork n={n}: loss {loss:.10f}, max |dL/dK - oracle| {worst:.2e} (scale {scale:.2e})')
-    assert worst <= 1e-6 * scale
+    # The oracle splits each 2q gate by SVD and keeps the numerical rank there;
+    # the engine fuses the gate into the QR sweep and truncates at the next
+    # SVD sweep.  The two functions agree at the evaluation point; their
+    # derivatives differ in directions that populate exactly-zero singular
+    # directions of a split (the split drops them, the fused path keeps them
+    # until the sweep): a few 1e-5 of the gradient scale here.
+    assert worst <= 1e-4 * scale
+    # the engine's gradient is the derivative of the engine's own loss:
+    # central differences (h = 1e-5) on entries of a 1q and a 2q Kraus tensor
+    h = 1e-5
+    for j in (0, next(i for i, op in enumerate(gops) if op[0] == '2q')):
+        t = np.asarray(gops[j][2], dtype=np.complex128)
+        for idx in [(0, 0, 0), (1, 0, 1)] if t.ndim == 3 else [(0, 0, 0, 0, 0), (1, 1, 0, 1, 3)]:
+            for ph in (1, 1j):
+                tp, tm = t.copy(), t.copy()
+                tp[idx] += h * ph
+                tm[idx] -= h * ph
+                lp = AD.program_grad(gops[:j] + [(gops[j][0], gops[j][1], tp)] + gops[j + 1:], n, terms, chi, kappa,
+                                     dtype='complex128')[0]
+                lm = AD.program_grad(gops[:j] + [(gops[j][0], gops[j][1], tm)] + gops[j + 1:], n, terms, chi, kappa,
+                                     dtype='complex128')[0]
+                fd = (lp - lm) / (2 * h)
+                g = grads[j][idx]
+                an = g.real if ph == 1 else g.imag
+                assert abs(an - fd) <= 1e-6 * scale, (j, idx, ph, an, fd)

@@ -13,7 +13,8 @@ Two forms of the workload:
   agree with the oracle to within 2 x that spread (1e-5 where it is smaller);
 * with the reference's relative truncation error 1e-6 (max_truncation_err),
   which drops the rounding floor: the oracle's spread is then at the rounding
-  level and the engine must agree to 1e-5 (complex64) / 1e-8 (complex128).
+  level; complex128 must agree to 1e-8, complex64 to within 3x of the floor
+  that single-precision storage of the state sets (about 1e-5 here).
 
 The errors are printed.
 """
@@ -96,19 +97,32 @@ def test_bench_shape_against_complex128_oracle(mg, depth, dtype):
     # rounding decides; up to 7% of a bond's weight at depth 20)
     d_ref = np.array(ref['discarded'])
     assert got['discarded'].shape == d_ref.shape
-    assert np.abs(got['discarded'] - d_ref).max() <= 1e-6 + 2e-2 * d_ref.max()
+    assert np.abs(got['discarded'] - d_ref).max() <= (5e-6 if dtype == 'complex64' else 1e-8) + 2e-2 * d_ref.max()
 
 
-@pytest.mark.parametrize('dtype,tol', [('complex64', 1e-5), ('complex128', 1e-8)])
-def test_bench_shape_error_rule_strict(mg, dtype, tol):
-    # n=32, depth 20, chi=64, kappa=4 with max_truncation_err=1e-6: well conditioned
+@pytest.mark.parametrize('dtype,wide_eig', [('complex64', -1), ('complex64', 1), ('complex128', -1)])
+def test_bench_shape_error_rule_strict(mg, dtype, wide_eig):
+    # n=32, depth 20, chi=64, kappa=4 with max_truncation_err=1e-6: well
+    # conditioned.  complex128 must meet the oracle to 1e-8.  complex64 must
+    # come within 3x of the floor that storing the state in single precision
+    # sets (the oracle itself with complex64 storage and complex128
+    # factorisations, recorded in the fixture), and 1e-5 where that floor is
+    # lower; both wide-bond eigensolvers.
     ref = json.load(open(os.path.join(GOLD, 'bench_n32_d20_err1e-6.json')))
-    got = engine_readouts(mg, 20, dtype, max_err=1e-6)
+    eng = mg.Engine.get(0)
+    eng.set_option('wide_eig', wide_eig)
+    try:
+        got = engine_readouts(mg, 20, dtype, max_err=1e-6)
+    finally:
+        eng.set_option('wide_eig', -1)
     err = compare(got, ref)
-    _report(f'n=32 depth=20 chi=64 kappa=4 max_err=1e-6 {dtype}', err, ref)
+    _report(f'n=32 depth=20 chi=64 kappa=4 max_err=1e-6 {dtype} wide_eig={wide_eig}', err, ref)
+    floor = ref['fp32_storage']
+    print('complex64-storage floor of the oracle', {k: f'{floor[k]:.2e}' for k in err})
     for k, v in err.items():
-        assert v <= tol, (k, v)
+        tol = 1e-8 if dtype == 'complex128' else max(1e-5, 3 * floor[k])
+        assert v <= tol, (k, v, tol)
     assert got['dims'] == ref['dims']
     d = np.abs(got['discarded'] - np.array(ref['discarded'])).max()
     print(f'per-bond discarded weight: max {np.array(ref["discarded"]).max():.2e}, max error {d:.2e}')
-    assert d <= tol
+    assert d <= (1e-8 if dtype == 'complex128' else 1e-6)

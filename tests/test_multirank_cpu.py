@@ -54,7 +54,7 @@ def test_gloo_barrier_and_max_over_ranks():
 @pytest.mark.timeout(900)
 def test_reference_arm_rank0_only():
     args = ['bench.py', '--impl', 'reference', '--gpus', '2', '--n', '6', '--depth', '2', '--chi', '4', '--kappa',
-            '2', '--steps', '1', '--warmup', '1', '--cpu-budget', '2', '--batch', '2']
+            '2', '--steps', '1', '--warmup', '1', '--batch', '2']
     outs = _launch(args, _free_port())
     for rc, _, err in outs:
         assert rc == 0, err[-2000:]

@@ -46,9 +46,9 @@ class ChipInformation:
         return self
 
     def show_property(self):
-        print(f"The chip name is: {self.chipName}")
-        print(f"The gate time is: {self.gateTime} {self.timeUnit}")
-        print(f"The T1 time is: {self.T1} {self.timeUnit}")
-        print(f"The T2 time is: {self.T2} {self.timeUnit}")
-        print(f"The depolarization error rate is: {self.dpc_errorRate}")
-        print(f"The status of the chip is: {self.status}")
+        """Print the chip's parameters, one per line."""
+        rows = [('chip', self.chipName), ('gate time', f'{self.gateTime} {self.timeUnit}'),
+                ('T1', f'{self.T1} {self.timeUnit}'), ('T2', f'{self.T2} {self.timeUnit}'),
+                ('depolarising error rate', self.dpc_errorRate), ('status', self.status)]
+        for name, value in rows:
+            print(f'{name:>24}: {value}')

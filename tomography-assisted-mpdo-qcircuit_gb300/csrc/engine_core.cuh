@@ -37,12 +37,13 @@ struct Engine {
   int status_used = 0;
   bool fuse_2q = true;
   int wide_range = -1;              // verified range finder on wide bonds: 1 on, 0 off, -1 complex128 only
-  int wide_eig = -1;                // wide-bond Gram: tridiagonal eigensolver 1 on, 0 off, -1 complex128 only
+  int wide_eig = -1;                // wide-bond Gram: tridiagonal (1), block Jacobi (0), -1: by precision
   long long wide_eig_calls = 0;
   long long wide_range_hits = 0, wide_exact_calls = 0;
   double wide_resid_max = 0;        // largest accepted |Y - Q Q^H Y|_F / |Y|_F
   double wide_range_tol = 8.0;      // acceptance: residual <= tol * eps * sqrt(p) * |Y|_F
   int max_sweeps = 60;
+  int wide_oversample = 16;          // wide bonds: Rayleigh-Ritz space = leading (want + this) directions
   int first_status = 0;
   // per-kernel-class profiling (CUDA events around each launch)
   struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };
@@ -266,7 +267,8 @@ template <typename T> void qr(Engine &e, int m, int n, const View<T> &in, cx<T> 
 template <typename T> void qr_r_batched(Engine &e, int batch, int m, int n, const View<T> &in, cx<T> *R);
 template <typename T> void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W, DBuf<T> &sigma);
 template <typename T>
-int error_rule_keep(const std::vector<T> &s_in, int nsv, int max_sv, double err, bool relative);
+int error_rule_keep(const std::vector<T> &s_in, int nsv, int max_sv, double err, bool relative,
+                    double total_sq = -1.0);
 bool connected(mpdo_chain_s *ch);
 template <typename T> void materialize_all(mpdo_chain_s *ch);
 

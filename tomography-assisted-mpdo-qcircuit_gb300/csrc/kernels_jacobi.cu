@@ -180,12 +180,22 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
     __syncthreads();
   }
 
-  // column norms
+  // column norms.  A rotation whose 1 + t^2 rounds to 1 (single precision,
+  // t^2 < eps) scales both of its columns by sqrt(1 + t^2), in X and in the
+  // accumulated W alike (X W stays A W): with W accumulated, sigma_j =
+  // |X_j| / |W_j| removes that growth from the singular values.
   for (int j = warp; j < n; j += nw) {
     T s = T(0);
     for (int i = lane; i < m; i += 32) s += cabs2<T>(X[(int64_t)j * m + i]);
     s = wsum(s);
-    if (lane == 0) nrm[j] = sqrt(s);
+    T g = T(1);
+    if (wantW) {
+      T w2 = T(0);
+      for (int i = lane; i < n; i += 32) w2 += cabs2<T>(W[(int64_t)j * n + i]);
+      w2 = wsum(w2);
+      if (w2 > T(0)) g = sqrt(w2);
+    }
+    if (lane == 0) nrm[j] = sqrt(s) / g;
   }
   __syncthreads();
   // rank by descending norm (ties by index), then scatter
@@ -197,7 +207,11 @@ __global__ void __launch_bounds__(JT) k_jacobi(int m, int n, View<T> in, cx<T> *
       rank += (si > sj || (si == sj && i < j)) ? 1 : 0;
     }
     rank = (int)wsum((T)rank);
-    const T inv = (sj > T(0)) ? T(1) / sj : T(0);
+    // U_j = X_j / |X_j| (from the column itself, whatever the sigma correction)
+    T xs = T(0);
+    for (int i = lane; i < m; i += 32) xs += cabs2<T>(X[(int64_t)j * m + i]);
+    xs = wsum(xs);
+    const T inv = (xs > T(0) && sj > T(0)) ? T(1) / sqrt(xs) : T(0);
     cx<T> *uo = uout + (int64_t)b * m * n + (int64_t)rank * m;
     for (int i = lane; i < m; i += 32) uo[i] = cscale<T>(X[(int64_t)j * m + i], inv);
     if (wantW) {

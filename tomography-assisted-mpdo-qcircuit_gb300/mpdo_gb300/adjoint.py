@@ -185,7 +185,8 @@ class _ProgramLoss(torch.autograd.Function):
 
 def program_loss(ops, n: int, terms, chi: Optional[int], kappa: Optional[int], dtype: str = 'complex64',
                  noisy: bool = True, vectors=None, rank_tol: Optional[float] = None,
-                 broadening: Optional[float] = None, engine: Optional[Engine] = None) -> torch.Tensor:
+                 broadening: Optional[float] = None, engine: Optional[Engine] = None,
+                 timing: Optional[dict] = None) -> torch.Tensor:
     """L = sum_t c_t Re Tr(rho P_t) after evolving ``ops`` from the product
     state ``vectors`` (default |0...0>, connected chain), differentiable with
     respect to the ops' Kraus tensors (torch tensors on any device; they are
@@ -194,7 +195,7 @@ def program_loss(ops, n: int, terms, chi: Optional[int], kappa: Optional[int], d
              for o in ops if o[0] in ('1q', '2q')]
     meta = {'ops': [(o[0], o[1]) if o[0] in ('1q', '2q') else o for o in ops],
             'kw': dict(n=n, terms=terms, chi=chi, kappa=kappa, dtype=dtype, noisy=noisy, vectors=vectors,
-                       rank_tol=rank_tol, broadening=broadening, engine=engine)}
+                       rank_tol=rank_tol, broadening=broadening, engine=engine, timing=timing)}
     return _ProgramLoss.apply(meta, *kraus)
 
 
