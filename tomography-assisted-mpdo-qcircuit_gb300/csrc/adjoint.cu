@@ -624,6 +624,7 @@ void program_grad(mpdo_engine_s *eng, const mpdo_program *prog, const int *Dd, c
   chain.s.assign(n, Site{});
   chain.bond.assign(std::max(0, n - 1), 1);
   chain.pend.assign(std::max(0, n - 1), Pend{});
+  chain.pend1.assign(n, Pend{});
   for (int i = 0; i < n; ++i) {
     cx<T> h[2] = {cmk<T>((T)prog->vectors[4 * i], (T)prog->vectors[4 * i + 1]),
                   cmk<T>((T)prog->vectors[4 * i + 2], (T)prog->vectors[4 * i + 3])};

@@ -505,23 +505,101 @@ int error_rule_keep(const std::vector<T> &s_in, int nsv, int max_sv, double err,
 // -------------------------------------------------------------- ops -----
 template <typename T> static void materialize_pair(mpdo_chain_s *ch, int i);
 
-template <typename T> static void materialize_touching(mpdo_chain_s *ch, int site) {
-  if (site - 1 >= 0 && ch->pend[site - 1].on) materialize_pair<T>(ch, site - 1);
-  if (site < ch->n - 1 && ch->pend[site].on) materialize_pair<T>(ch, site);
-}
-template <typename T> void materialize_all(mpdo_chain_s *ch) {
-  for (int i = 0; i + 1 < ch->n; ++i)
-    if (ch->pend[i].on) materialize_pair<T>(ch, i);
+// Deferred single-qubit gates.  A 1q Kraus map with sum_k K_k^H K_k = I
+// (trace preserving) acts on a site's physical and Kraus legs as an isometry
+// B (I_l (x) G (x) I_r with G^H G = I on the (s, a) legs): the QR factor R of
+// B A equals that of A, and the left singular vectors and values of a bond
+// matrix B Y equal those of Y.  A truncate that follows a 1q sublayer
+// therefore runs its QR and SVD sweeps on the pre-gate sites (K times fewer
+// rows or columns) and applies the Kraus maps afterwards, before the kappa
+// pass; the keep counts use the post-gate dimensions (the extra singular
+// values are exact zeros and are zero-padded as the reference keeps them).
+// Any other operation on the site applies the map first.
+static bool trace_preserving(const double *g, int K, double tol) {
+  for (int s = 0; s < 2; ++s)
+    for (int t = 0; t < 2; ++t) {
+      double re = 0, im = 0;
+      for (int x = 0; x < 2; ++x)
+        for (int k = 0; k < K; ++k) {
+          const double *a = g + 2 * ((x * 2 + s) * K + k), *b = g + 2 * ((x * 2 + t) * K + k);
+          re += a[0] * b[0] + a[1] * b[1];       // conj(a) b
+          im += a[0] * b[1] - a[1] * b[0];
+        }
+      if (std::fabs(re - (s == t ? 1.0 : 0.0)) > tol || std::fabs(im) > tol) return false;
+    }
+  return true;
 }
 
-template <typename T> static void apply_1q(mpdo_chain_s *ch, int site, const double *kraus, int K) {
+template <typename T> static void kraus_site(mpdo_chain_s *ch, int site, const double *kraus, int K) {
   Engine &e = ch->eng->e;
-  materialize_touching<T>(ch, site);
   const Site s = ch->s[site];
   DBuf<cx<T>> out(e, (size_t)s.l * 2 * s.a * K * s.r);
   prof(e, K_KRAUS1Q, 8.0 * 2 * 2 * K * s.elems(), (double)sizeof(cx<T>) * s.elems() * (1 + K),
        [&] { kraus1q<T>(e.stream, site_ptr<T>(ch, site), out.p, s.l, s.a, s.r, kraus, K); });
   set_site<T>(ch, site, out.release(), s.l, s.a * K, s.r);
+}
+
+template <typename T> static void materialize_1q(mpdo_chain_s *ch, int site) {
+  Pend &p = ch->pend1[site];
+  if (!p.on) return;
+  p.on = false;
+  kraus_site<T>(ch, site, p.t.data(), p.K);
+}
+template <typename T> static void materialize_1q_all(mpdo_chain_s *ch) {
+  for (int i = 0; i < ch->n; ++i) materialize_1q<T>(ch, i);
+}
+// Kraus-leg dimension of a site once its deferred map is applied
+static int a_eff(const mpdo_chain_s *ch, int i) { return ch->s[i].a * (ch->pend1[i].on ? ch->pend1[i].K : 1); }
+
+template <typename T> static void materialize_touching(mpdo_chain_s *ch, int site) {
+  if (site - 1 >= 0 && ch->pend[site - 1].on) materialize_pair<T>(ch, site - 1);
+  if (site < ch->n - 1 && ch->pend[site].on) materialize_pair<T>(ch, site);
+  materialize_1q<T>(ch, site);
+}
+template <typename T> void materialize_all(mpdo_chain_s *ch) {
+  for (int i = 0; i + 1 < ch->n; ++i)
+    if (ch->pend[i].on) materialize_pair<T>(ch, i);
+  materialize_1q_all<T>(ch);
+}
+
+template <typename T> static void apply_1q(mpdo_chain_s *ch, int site, const double *kraus, int K) {
+  Engine &e = ch->eng->e;
+  // pending pairs on this site are older than the gate
+  if (site - 1 >= 0 && ch->pend[site - 1].on) materialize_pair<T>(ch, site - 1);
+  if (site < ch->n - 1 && ch->pend[site].on) materialize_pair<T>(ch, site);
+  const double tol = sizeof(T) == 4 ? 1e-6 : 1e-12;
+  Pend &p = ch->pend1[site];
+  if (e.defer_1q && trace_preserving(kraus, K, tol)) {
+    if (p.on && p.K * K <= 16) {
+      // compose: G[x][s][k1 K + k2] = sum_y G2[x][y][k2] G1[y][s][k1] (old Kraus index first)
+      const int K1 = p.K, KK = K1 * K;
+      std::vector<double> g(2 * 4 * KK, 0.0);
+      for (int x = 0; x < 2; ++x)
+        for (int s = 0; s < 2; ++s)
+          for (int k1 = 0; k1 < K1; ++k1)
+            for (int k2 = 0; k2 < K; ++k2) {
+              double re = 0, im = 0;
+              for (int y = 0; y < 2; ++y) {
+                const double *a = kraus + 2 * ((x * 2 + y) * K + k2), *b = p.t.data() + 2 * ((y * 2 + s) * K1 + k1);
+                re += a[0] * b[0] - a[1] * b[1];
+                im += a[0] * b[1] + a[1] * b[0];
+              }
+              double *o = g.data() + 2 * ((x * 2 + s) * KK + k1 * K + k2);
+              o[0] = re;
+              o[1] = im;
+            }
+      p.t.swap(g);
+      p.K = KK;
+      return;
+    }
+    materialize_1q<T>(ch, site);
+    p.on = true;
+    p.t.assign(kraus, kraus + 8 * K);
+    p.K = K;
+    return;
+  }
+  materialize_1q<T>(ch, site);
+  kraus_site<T>(ch, site, kraus, K);
 }
 
 template <typename T> static void materialize_pair(mpdo_chain_s *ch, int i) {
@@ -555,6 +633,8 @@ template <typename T> static void materialize_pair(mpdo_chain_s *ch, int i) {
 template <typename T> static void apply_2q(mpdo_chain_s *ch, int i, const double *t, int K, double cutoff) {
   for (int j = std::max(0, i - 1); j <= std::min(ch->n - 2, i + 1); ++j)
     if (ch->pend[j].on) materialize_pair<T>(ch, j);
+  materialize_1q<T>(ch, i);
+  materialize_1q<T>(ch, i + 1);
   Pend &p = ch->pend[i];
   p.on = true;
   p.t.assign(t, t + 32 * K);
@@ -645,9 +725,11 @@ template <typename T> static void svd_sweep(mpdo_chain_s *ch, int chi, double ma
   for (int idx = ch->n - 1; idx >= 1; --idx) {
     const Site P = ch->s[idx - 1], S = ch->s[idx];
     const int b = S.l, Nc = 2 * S.a * S.r;
-    const int rows_prev = P.l * 2 * P.a;
+    // the reference's keep rule sees the post-gate dimensions of deferred sites
+    const int rows_prev = P.l * 2 * a_eff(ch, idx - 1);
+    const int Nc_eff = 2 * a_eff(ch, idx) * S.r;
     auto keep_fn = [&](const T *s_dev, int) -> int {
-      const int nsv = std::min(rows_prev, Nc);
+      const int nsv = std::min(rows_prev, Nc_eff);
       const int cap = chi > 0 ? std::min(chi, nsv) : nsv;
       if (max_err < 0) return cap;
       std::vector<T> s(std::min(b, Nc));
@@ -661,13 +743,17 @@ template <typename T> static void svd_sweep(mpdo_chain_s *ch, int chi, double ma
     };
     DBuf<cx<T>> Lf, Rf;
     int keep = 0;
-    const int want = chi > 0 ? std::min(chi, std::min(rows_prev, Nc)) : -1;
-    // the kept count never exceeds the chi cap, with or without an error
-    // rule, so a wide bond only needs its leading `want` directions refined
+    const int want = chi > 0 ? std::min(chi, std::min(rows_prev, Nc_eff)) : -1;
+    // under the chi cap alone a wide bond refines its leading want + 16
+    // directions (Rayleigh-Ritz); under an error rule, whose cut is decided by
+    // the smallest kept values, all of them (measured on the n=32, chi=64,
+    // kappa=4 circuit with max_err = 1e-6, complex64: 2e-6 against the
+    // complex128 oracle with the full space, 2e-5 with want + 16)
     svd_split<T>(e, site_ptr<T>(ch, idx), b, Nc, keep_fn, Lf, Rf, keep, wdev ? wdev + 2 * (idx - 1) : nullptr,
-                 want);
-    DBuf<cx<T>> NP(e, (size_t)rows_prev * keep);
-    gemm<T>(e, rows_prev, keep, b, RM<T>(site_ptr<T>(ch, idx - 1), b), RM<T>(Lf.p, keep), NP.p, keep);
+                 max_err < 0 ? want : -1);
+    const int prow = P.l * 2 * P.a;
+    DBuf<cx<T>> NP(e, (size_t)prow * keep);
+    gemm<T>(e, prow, keep, b, RM<T>(site_ptr<T>(ch, idx - 1), b), RM<T>(Lf.p, keep), NP.p, keep);
     set_site<T>(ch, idx - 1, NP.release(), P.l, P.a, keep);
     set_site<T>(ch, idx, Rf.release(), keep, S.a, S.r);
   }
@@ -760,8 +846,13 @@ static void truncate_layer(mpdo_chain_s *ch, int chi, int kappa, double max_err,
   if (chi > 0 || max_err >= 0) {
     if (disc_out && ch->n > 1) w = DBuf<double>(e, (size_t)2 * (ch->n - 1));
     if (!e.fuse_2q) materialize_all<T>(ch);
+    // a deferred site whose QR would keep fewer columns before the gate than
+    // after it (rows < right bond, the chain ends) is applied first
+    for (int i = 0; i + 1 < ch->n; ++i)
+      if (ch->pend1[i].on && ch->s[i].l * 2 * ch->s[i].a < ch->s[i].r) materialize_1q<T>(ch, i);
     qr_sweep<T>(ch);
     svd_sweep<T>(ch, chi, max_err, w.p);
+    materialize_1q_all<T>(ch);
   }
   if (noisy) {
     materialize_all<T>(ch);
@@ -1074,6 +1165,7 @@ template <typename T> static void read_site(mpdo_chain_s *ch, int site, double *
 
 template <typename T> static void write_site(mpdo_chain_s *ch, int site, const int dims[4], const double *in) {
   Engine &e = ch->eng->e;
+  ch->pend1[site].on = false;                 // replaced by the written tensor
   materialize_touching<T>(ch, site);
   const size_t n = (size_t)dims[0] * 2 * dims[2] * dims[3];
   std::vector<cx<T>> h(n);
@@ -1215,6 +1307,7 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
     const std::string k(name);
     Engine &e = eng->e;
     if (k == "fuse_2q") e.fuse_2q = value != 0;
+    else if (k == "defer_1q") e.defer_1q = value != 0;
     else if (k == "wide_range") e.wide_range = value > 0 ? 1 : (value < 0 ? -1 : 0);
     else if (k == "wide_eig") e.wide_eig = value > 0 ? 1 : (value < 0 ? -1 : 0);
     else if (k == "wide_range_tol") {
@@ -1314,6 +1407,7 @@ mpdo_status mpdo_chain_create(mpdo_engine_t eng, int n, int dtype, const double 
     ch->s.assign(n, Site{});
     ch->bond.assign(std::max(0, n - 1), connected_ ? 1 : 0);
     ch->pend.assign(std::max(0, n - 1), Pend{});
+    ch->pend1.assign(n, Pend{});
     if (dtype == MPDO_C64) chain_init<float>(ch.get(), vectors);
     else chain_init<double>(ch.get(), vectors);
     *out = ch.release();

@@ -36,6 +36,7 @@ struct Engine {
   int status_cap = 8192;
   int status_used = 0;
   bool fuse_2q = true;
+  bool defer_1q = true;              // trace-preserving 1q channels deferred past the truncate sweeps
   int wide_range = -1;              // verified range finder on wide bonds: 1 on, 0 off, -1 complex128 only
   int wide_eig = -1;                // wide-bond Gram: tridiagonal (1), block Jacobi (0), -1: by precision
   long long wide_eig_calls = 0;
@@ -219,6 +220,7 @@ struct mpdo_chain_s {
   std::vector<mpdo::Site> s;
   std::vector<char> bond;
   std::vector<mpdo::Pend> pend;
+  std::vector<mpdo::Pend> pend1;     // deferred trace-preserving 1q Kraus maps, per site
 };
 
 namespace mpdo {
