@@ -41,6 +41,22 @@ static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 
 // ---------------------------------------------------------------- QR ----
+// Rows per TSQR chunk of an m x n level: the whole level if it fits shared
+// memory; else the largest multiple of 32 that fits (with the explicit-Q
+// pass and its two reflector buffers) and exceeds n, so that every level
+// shrinks the stacked R; and when no shared-memory chunk can exceed n (wide
+// factors, n > ~100 in complex64), chunks of 2n rows factored in global
+// memory (L2 resident), so that the level still splits across CTAs instead of
+// one CTA sweeping all m rows.
+static int tsqr_chunk_rows(int m, int n, size_t esz, size_t cap) {
+  if ((size_t)m * (n + 2) * esz <= cap) return m;
+  size_t mcs = cap / ((size_t)(n + 2) * esz);
+  mcs = mcs / 32 * 32;
+  if (mcs > (size_t)n) return (int)std::min<size_t>(mcs, (size_t)m);
+  const int g = (2 * n + 31) / 32 * 32;
+  return m > g ? g : m;
+}
+
 // Householder QR of an m x n matrix (view `in`): Q (m x k, row-major, ld k),
 // R (k x n row-major), k = min(m, n).  Tall-skinny inputs go through TSQR
 // levels of shared-memory-resident chunks.
@@ -60,13 +76,7 @@ void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
     // largest multiple of 32 that fits (with the explicit-Q pass and its two
     // reflector buffers) and exceeds
     // n, so that every level shrinks the stacked R; else one global chunk
-    int mc;
-    if ((size_t)curm * (n + 2) * esz <= cap) mc = curm;
-    else {
-      size_t mcs = cap / ((size_t)(n + 2) * esz);
-      mcs = mcs / 32 * 32;
-      mc = (mcs > (size_t)n) ? (int)std::min<size_t>(mcs, (size_t)curm) : curm;
-    }
+    int mc = tsqr_chunk_rows(curm, n, esz, cap);
     const int nch = (curm + mc - 1) / mc;
     Level L;
     L.m = curm; L.mc = mc; L.nch = nch;
@@ -129,13 +139,7 @@ void qr_r_batched(Engine &e, int batch, int m, int n, const View<T> &in, cx<T> *
   View<T> cur = in;
   int curm = m, last_nch = 1;
   while (true) {
-    int mc;
-    if ((size_t)curm * (n + 2) * esz <= cap) mc = curm;
-    else {
-      size_t mcs = cap / ((size_t)(n + 2) * esz);
-      mcs = mcs / 32 * 32;
-      mc = (mcs > (size_t)n) ? (int)std::min<size_t>(mcs, (size_t)curm) : curm;
-    }
+    int mc = tsqr_chunk_rows(curm, n, esz, cap);
     const int nch = (curm + mc - 1) / mc;
     v = DBuf<cx<T>>(e, (size_t)batch * nch * mc * n);
     tau = DBuf<cx<T>>(e, (size_t)batch * nch * n);
