@@ -152,6 +152,21 @@ mpdo_status mpdo_truncate(mpdo_chain_t ch, int chi, int kappa, double max_err, i
                           double *discarded_out);
 mpdo_status mpdo_kappa_truncate(mpdo_chain_t ch, int kappa, double max_err);
 
+/* The reference's sweeps one at a time on a connected chain:
+ *   mpdo_qr_left2right   TNNOptimizer.py:87-108 (reduced QR per site, R absorbed
+ *                        into the next site; no truncation)
+ *   mpdo_svd_right2left  TNNOptimizer.py:111-134 and
+ *   mpdo_svd_left2right  TNNOptimizer.py:137-161: per bond, the SVD of the
+ *                        contracted pair keeping <= chi values (chi <= 0: no
+ *                        cap) and the relative error rule (max_err < 0: none),
+ *                        sqrt(S) on both factors.  The pair is decomposed
+ *                        exactly without forming it (QR / LQ of the other
+ *                        site first).  discarded_out (nullable, n-1 doubles):
+ *                        per-bond discarded weight. */
+mpdo_status mpdo_qr_left2right(mpdo_chain_t ch);
+mpdo_status mpdo_svd_right2left(mpdo_chain_t ch, int chi, double max_err, double *discarded_out);
+mpdo_status mpdo_svd_left2right(mpdo_chain_t ch, int chi, double max_err, double *discarded_out);
+
 /* Reduced density matrix on `keep` (m ascending qubit indices; m <= 14):
  * 2^m x 2^m complex, rows = ket (qubit keep[0] most significant). */
 mpdo_status mpdo_reduced_dm(mpdo_chain_t ch, const int *keep, int m, double *host_out);

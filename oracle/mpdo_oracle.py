@@ -478,6 +478,27 @@ def svd_right2left(st: MPDO, chi: Optional[int], max_err: Optional[float],
     return disc
 
 
+def svd_left2right(st: MPDO, chi: Optional[int], max_err: Optional[float]) -> List[float]:
+    """TNNOptimizer.py:137-161: the mirror sweep, pairs (idx, idx+1) for idx =
+    0 .. n-2, the same split (<= chi, relative error rule, sqrt(S) on both
+    sides).  Returns the discarded weight per bond."""
+    disc = [0.0] * (st.n - 1)
+    for idx in range(st.n - 1):
+        a, b = st.sites[idx], st.sites[idx + 1]
+        l, x, aa, _ = a.shape
+        _, y, cc, r = b.shape
+        m = torch.einsum('lsam,mtcr->lsatcr', a, b).reshape(l * x * aa, y * cc * r)
+        u, s, vh, rest = svd_truncate(m, chi, max_err, relative=True)
+        tot = float((s ** 2).sum() + (rest ** 2).sum())
+        disc[idx] = float((rest ** 2).sum()) / tot if tot > 0 else 0.0
+        ss = torch.sqrt(s).to(m.dtype)
+        k = s.numel()
+        st.sites[idx] = (u * ss[None, :]).reshape(l, x, aa, k)
+        st.sites[idx + 1] = (ss[:, None] * vh).reshape(k, y, cc, r)
+    st.discarded = disc
+    return disc
+
+
 def svd_kappa(st: MPDO, kappa: Optional[int], max_err: Optional[float],
               randomized: bool = False) -> None:
     """TNNOptimizer.py:164-197: per site with dim(I_k) > kappa, SVD of

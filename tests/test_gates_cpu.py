@@ -160,6 +160,13 @@ class _FakeChain:
     def kappa_truncate(self, *a):
         self.calls.append(('kappa',) + a)
 
+    def qr_left2right(self):
+        self.calls.append(('qr',))
+
+    def svd_sweep(self, *a):
+        self.calls.append(('svd',) + a)
+        return [0.0] * (self.n - 1)
+
 
 def test_tnnoptimizer_entry_points_map_to_engine_operations():
     # TNNOptimizer.py:51-197 on the nodes of an evolved state
@@ -180,5 +187,10 @@ def test_tnnoptimizer_entry_points_map_to_engine_operations():
         T.bondTruncate(tuple(nodes), 4)
     with pytest.raises(ValueError):
         T.bondTruncate(nodes[:2], 4)
-    with pytest.raises(NotImplementedError):
-        T.qr_left2right(nodes)
+    ch.calls.clear()
+    T.qr_left2right(nodes)
+    assert T.svd_right2left(nodes, 4) == [0.0, 0.0]
+    T.svd_left2right(nodes, 2, 1e-6)
+    assert ch.calls == [('qr',), ('svd', 'right2left', 4, None), ('svd', 'left2right', 2, 1e-6)]
+    with pytest.raises(ValueError):
+        T.svd_left2right(nodes[:1], 2)

@@ -5,9 +5,10 @@ The functions take the ``stateNodes`` that ``TensorCircuit.evolve`` hands
 out and act on the GPU chain behind them, in place, as the reference's act
 on its node list.  The engine runs the reference's QR left-to-right and SVD
 right-to-left sweeps as one operation (``bondTruncate``) and the kappa pass
-as another (``svdKappa_left2right``).  The sweeps are not offered one at a
-time: ``qr_left2right`` alone only changes the gauge, and the evolution
-never calls ``svd_right2left`` or ``svd_left2right`` on their own.
+as another (``svdKappa_left2right``); the three sweeps are also offered one
+at a time (``qr_left2right``, ``svd_right2left``, ``svd_left2right``).  Each
+needs a connected chain, as the reference's do (they look up the shared
+bond edges).
 """
 from typing import List, Optional
 
@@ -64,18 +65,27 @@ def svdKappa_left2right(_qubits: List[QubitNode], max_singular_values: Optional[
     _chain(_qubits, 'svdKappa_left2right').kappa_truncate(max_singular_values, max_truncation_err)
 
 
-def _single_sweep(name: str):
-    def f(*args, **kwargs):
-        raise NotImplementedError(f'`{name}` alone is not offered by the GB300 engine: bondTruncate runs the '
-                                  'QR left-to-right and SVD right-to-left sweeps as one operation')
-    f.__name__ = name
-    f.__doc__ = f'TNNOptimizer.py `{name}`: not offered on its own (see bondTruncate).'
-    return f
+def qr_left2right(_qubits: List[QubitNode]):
+    """TNNOptimizer.py:87-108: reduced QR of every site but the last over
+    (left bond, physical, Kraus) x (right bond), R absorbed into the next
+    site.  Changes the gauge only."""
+    _chain(_qubits, 'qr_left2right').qr_left2right()
 
 
-qr_left2right = _single_sweep('qr_left2right')
-svd_right2left = _single_sweep('svd_right2left')
-svd_left2right = _single_sweep('svd_left2right')
+def svd_right2left(_qubits: List[QubitNode], max_singular_values: Optional[int] = None,
+                   max_truncation_err: Optional[float] = None):
+    """TNNOptimizer.py:111-134: for idx = n-1 .. 1, split the contracted pair
+    (idx-1, idx) keeping at most ``max_singular_values`` (and the relative
+    error rule), sqrt(S) on both sides.  Returns the discarded weight per
+    bond (the reference drops it)."""
+    return _chain(_qubits, 'svd_right2left').svd_sweep('right2left', max_singular_values, max_truncation_err)
+
+
+def svd_left2right(_qubits: List[QubitNode], max_singular_values: int,
+                   max_truncation_err: Optional[float] = None):
+    """TNNOptimizer.py:137-161: the same split over the pairs (idx, idx+1) for
+    idx = 0 .. n-2."""
+    return _chain(_qubits, 'svd_left2right').svd_sweep('left2right', max_singular_values, max_truncation_err)
 
 
 def cal_entropy(qubits):

@@ -763,6 +763,123 @@ template <typename T> static void svd_sweep(mpdo_chain_s *ch, int chi, double ma
   }
 }
 
+// ------------------------------------------------ standalone sweeps ----
+// The reference's sweeps called one at a time on an arbitrary chain
+// (TNNOptimizer.py:87-161).  The SVD sweeps decompose the contracted pair
+// M = A_{idx-1} A_idx exactly without forming it: the neighbour that the
+// step does not keep is factored first (QR of the left site for the
+// right-to-left sweep, LQ of the right site for the left-to-right one), and
+// only the small remainder is decomposed.  Keep counts follow the pair's
+// shape (min(chi, rows, cols) including zero singular values, the relative
+// error rule), sqrt(S) goes on both factors.
+
+// TNNOptimizer.py:87-108
+template <typename T> static void qr_left2right_only(mpdo_chain_s *ch) {
+  materialize_all<T>(ch);
+  qr_sweep<T>(ch);
+}
+
+template <typename T>
+static int sweep_keep(Engine &e, const T *s_dev, int len, int nsv, int chi, double max_err, const cx<T> *Y,
+                      size_t ny) {
+  const int cap = chi > 0 ? std::min(chi, nsv) : nsv;
+  if (max_err < 0) return cap;
+  std::vector<T> s(len);
+  DBuf<double> tot(e, 1);
+  sumsq<T>(e.stream, Y, ny, tot.p);
+  double htot = 0;
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(s.data(), s_dev, s.size() * sizeof(T), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(&htot, tot.p, sizeof(double), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  return error_rule_keep<T>(s, nsv, cap, max_err, true, htot);
+}
+
+static void discarded_to_host(Engine &e, const DBuf<double> &w, int nb, double *out) {
+  if (!out) return;
+  std::vector<double> h(2 * (size_t)nb);
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), w.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  for (int i = 0; i < nb; ++i) out[i] = h[2 * i + 1] > 0 ? (h[2 * i + 1] - h[2 * i]) / h[2 * i + 1] : 0.0;
+}
+
+// TNNOptimizer.py:111-134: for idx = n-1 .. 1, A_{idx-1} = Q R, Y = R A_idx,
+// Y = U S V^H: A_{idx-1} := Q U sqrt(S), A_idx := sqrt(S) V^H
+template <typename T> static void svd_right2left_only(mpdo_chain_s *ch, int chi, double max_err, double *disc) {
+  Engine &e = ch->eng->e;
+  materialize_all<T>(ch);
+  const int n = ch->n;
+  DBuf<double> w(e, (size_t)2 * std::max(1, n - 1));
+  MPDO_CUDA_CHECK(cudaMemsetAsync(w.p, 0, sizeof(double) * 2 * std::max(1, n - 1), e.stream));
+  for (int idx = n - 1; idx >= 1; --idx) {
+    const Site P = ch->s[idx - 1], S = ch->s[idx];
+    const int rows = P.l * 2 * P.a, m = P.r, Nc = 2 * S.a * S.r, kq = std::min(rows, m);
+    DBuf<cx<T>> Q(e, (size_t)rows * kq), R(e, (size_t)kq * m), Y(e, (size_t)kq * Nc);
+    qr<T>(e, rows, m, RM<T>(site_ptr<T>(ch, idx - 1), m), Q.p, R.p);
+    gemm<T>(e, kq, Nc, m, RM<T>(R.p, m), RM<T>(site_ptr<T>(ch, idx), Nc), Y.p, Nc);
+    const int nsv = std::min(rows, Nc);
+    auto keep_fn = [&](const T *s_dev, int) -> int {
+      return sweep_keep<T>(e, s_dev, std::min(kq, Nc), nsv, chi, max_err, Y.p, (size_t)kq * Nc);
+    };
+    DBuf<cx<T>> Lf, Rf;
+    int keep = 0;
+    svd_split<T>(e, Y.p, kq, Nc, keep_fn, Lf, Rf, keep, w.p + 2 * (idx - 1),
+                 max_err < 0 && chi > 0 ? std::min(chi, nsv) : -1);
+    DBuf<cx<T>> NP(e, (size_t)rows * keep);
+    gemm<T>(e, rows, keep, kq, RM<T>(Q.p, kq), RM<T>(Lf.p, keep), NP.p, keep);
+    set_site<T>(ch, idx - 1, NP.release(), P.l, P.a, keep);
+    set_site<T>(ch, idx, Rf.release(), keep, S.a, S.r);
+  }
+  discarded_to_host(e, w, n - 1, disc);
+}
+
+// TNNOptimizer.py:137-161: for idx = 0 .. n-2, A_{idx+1} = L Q (LQ: QR of
+// its adjoint), Y = A_idx L, Y = U S V^H: A_idx := U sqrt(S),
+// A_{idx+1} := sqrt(S) V^H Q
+template <typename T> static void svd_left2right_only(mpdo_chain_s *ch, int chi, double max_err, double *disc) {
+  Engine &e = ch->eng->e;
+  materialize_all<T>(ch);
+  const int n = ch->n;
+  DBuf<double> w(e, (size_t)2 * std::max(1, n - 1));
+  MPDO_CUDA_CHECK(cudaMemsetAsync(w.p, 0, sizeof(double) * 2 * std::max(1, n - 1), e.stream));
+  for (int idx = 0; idx + 1 < n; ++idx) {
+    const Site A = ch->s[idx], B = ch->s[idx + 1];
+    const int rows = A.l * 2 * A.a, m = A.r, cols = 2 * B.a * B.r, kq = std::min(cols, m);
+    // B (m x cols) = Lq Qh with B^H = Q0 R0: Lq = R0^H (m x kq), Qh = Q0^H (kq x cols)
+    DBuf<cx<T>> Q0(e, (size_t)cols * kq), R0(e, (size_t)kq * m);
+    qr<T>(e, cols, m, CM<T>(site_ptr<T>(ch, idx + 1), cols, 1), Q0.p, R0.p);
+    DBuf<cx<T>> Y(e, (size_t)rows * kq);
+    gemm<T>(e, rows, kq, m, RM<T>(site_ptr<T>(ch, idx), m), CM<T>(R0.p, m, 1), Y.p, kq);   // A_idx R0^H
+    const int nsv = std::min(rows, cols);
+    // Y is tall (rows >= kq in practice): its right singular vectors by QR +
+    // one-sided Jacobi, then L = U sqrt(S) = Y V S^-1/2, R = sqrt(S) V^H
+    DBuf<cx<T>> W;
+    DBuf<T> sg;
+    right_svd<T>(e, rows, kq, RM<T>(Y.p, kq), W, sg);                 // W: kq x kq column-major
+    const int keep = sweep_keep<T>(e, sg.p, kq, nsv, chi, max_err, Y.p, (size_t)rows * kq);
+    const int kk = std::min(keep, std::min(rows, kq));
+    sigma_weights<T>(e.stream, sg.p, kq, keep, w.p + 2 * idx);
+    sumsq<T>(e.stream, Y.p, (size_t)rows * kq, w.p + 2 * idx + 1);
+    DBuf<cx<T>> Lf(e, (size_t)rows * std::max(keep, 1)), Rf(e, (size_t)std::max(keep, 1) * kq);
+    if (keep > kk) {
+      fill_zero<T>(e.stream, Lf.p, (size_t)rows * keep);
+      fill_zero<T>(e.stream, Rf.p, (size_t)keep * kq);
+    }
+    if (kk > 0) {
+      gemm<T>(e, rows, kk, kq, RM<T>(Y.p, kq), CM<T>(W.p, kq), Lf.p, keep);              // Y V_k
+      scale_matrix<T>(e.stream, Lf.p, rows, kk, keep, sg.p, 0, 2);
+      const int64_t d[4] = {1, 1, kk, kq};
+      const int64_t st[4] = {0, 0, kq, 1};
+      copy4d<T>(e.stream, Rf.p, W.p, d, st, 1);                                            // V_k^H
+      scale_matrix<T>(e.stream, Rf.p, kk, kq, kq, sg.p, 1, 1);
+    }
+    DBuf<cx<T>> NB(e, (size_t)keep * cols);
+    gemm<T>(e, keep, cols, kq, RM<T>(Rf.p, kq), CM<T>(Q0.p, kq, 1), NB.p, cols);             // Rf Q0^H
+    set_site<T>(ch, idx, Lf.release(), A.l, A.a, keep);
+    set_site<T>(ch, idx + 1, NB.release(), keep, B.a, B.r);
+  }
+  discarded_to_host(e, w, n - 1, disc);
+}
+
 // TNNOptimizer.py:164-197: per site, SVD of (l,s,r) x a keeping kappa; the
 // site becomes U S = A V[:, :keep].  V comes from QR of A and one-sided
 // Jacobi on R.
@@ -1524,6 +1641,33 @@ mpdo_status mpdo_kappa_truncate(mpdo_chain_t ch, int kappa, double max_err) {
     set_device(ch->eng);
     DISPATCH(ch, materialize_all, ch);
     DISPATCH(ch, kappa_pass, ch, kappa, max_err);
+  });
+}
+
+mpdo_status mpdo_qr_left2right(mpdo_chain_t ch) {
+  return guard([&] {
+    need(ch != nullptr, "NULL argument");
+    need(connected(ch), "qr_left2right needs every neighbouring pair to share a bond");
+    set_device(ch->eng);
+    DISPATCH(ch, qr_left2right_only, ch);
+  });
+}
+
+mpdo_status mpdo_svd_right2left(mpdo_chain_t ch, int chi, double max_err, double *discarded_out) {
+  return guard([&] {
+    need(ch != nullptr, "NULL argument");
+    need(connected(ch), "svd_right2left needs every neighbouring pair to share a bond");
+    set_device(ch->eng);
+    DISPATCH(ch, svd_right2left_only, ch, chi, max_err, discarded_out);
+  });
+}
+
+mpdo_status mpdo_svd_left2right(mpdo_chain_t ch, int chi, double max_err, double *discarded_out) {
+  return guard([&] {
+    need(ch != nullptr, "NULL argument");
+    need(connected(ch), "svd_left2right needs every neighbouring pair to share a bond");
+    set_device(ch->eng);
+    DISPATCH(ch, svd_left2right_only, ch, chi, max_err, discarded_out);
   });
 }
 

@@ -64,6 +64,9 @@ SIGNATURES = {
     'mpdo_apply_2q': (_I, [_P, _I, _DP, _I, _D]),
     'mpdo_truncate': (_I, [_P, _I, _I, _D, _I, _DP]),
     'mpdo_kappa_truncate': (_I, [_P, _I, _D]),
+    'mpdo_qr_left2right': (_I, [_P]),
+    'mpdo_svd_right2left': (_I, [_P, _I, _D, _DP]),
+    'mpdo_svd_left2right': (_I, [_P, _I, _D, _DP]),
     'mpdo_reduced_dm': (_I, [_P, _IP, _I, _DP]),
     'mpdo_probs': (_I, [_P, _IP, _I, _DP]),
     'mpdo_expect_ops': (_I, [_P, _IP, _DP, _I, _DP]),

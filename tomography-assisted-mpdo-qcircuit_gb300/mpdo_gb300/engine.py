@@ -193,6 +193,18 @@ class Chain:
                                     out.ctypes.data_as(C.POINTER(C.c_int8))))
         return out
 
+    def qr_left2right(self) -> None:
+        """TNNOptimizer.py:87-108 on its own."""
+        check(self._lib.mpdo_qr_left2right(self.handle))
+
+    def svd_sweep(self, direction: str, chi: Optional[int], max_err: Optional[float]) -> np.ndarray:
+        """TNNOptimizer.py:111-161: 'right2left' or 'left2right' SVD sweep on
+        its own; returns the per-bond discarded weight."""
+        out = np.zeros(max(self.n - 1, 1), dtype=np.float64)
+        fn = self._lib.mpdo_svd_right2left if direction == 'right2left' else self._lib.mpdo_svd_left2right
+        check(fn(self.handle, int(chi or 0), -1.0 if max_err is None else float(max_err), _dptr(out)))
+        return out[: self.n - 1]
+
     def kappa_truncate(self, kappa: Optional[int], max_err: Optional[float]) -> None:
         check(self._lib.mpdo_kappa_truncate(self.handle, int(kappa or 0),
                                             -1.0 if max_err is None else float(max_err)))
