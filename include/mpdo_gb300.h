@@ -24,6 +24,7 @@
  *                          (single-site operator products)
  *   mpdo_expect_pauli_batch  many pauli_expect terms sharing one pass
  *   mpdo_sample            Circuit.py:297-446 sample (conditional sampling)
+ *   mpdo_sample_schemes    Circuit.py:448-466 randomSample (many schemes)
  *
  * Layout of a site tensor in device memory: complex, row-major
  * A[l][s][a][r] (l left bond, s physical = 2, a Kraus leg I_k, r right bond).
@@ -188,6 +189,18 @@ mpdo_status mpdo_expect_pauli_batch(mpdo_chain_t ch, const int8_t *paulis, int n
  * left environment advances in one batched step per measured qubit. */
 mpdo_status mpdo_sample(mpdo_chain_t ch, const int *order, int L, int64_t shots, uint64_t seed, double pfloor,
                         int8_t *bits_out);
+
+/* Circuit.py:448-466 randomSample: the same sampling in S measurement schemes
+ * in one call.  schemes is S x L (0: X, 1: Y, 2: Z per measured qubit), rot
+ * the MeasureX and MeasureY gates as two 2 x 2 complex matrices (8 doubles
+ * each, row-major (out, in); may be NULL when every basis is Z), seeds one
+ * per scheme, bits_out S x shots x L.  Scheme s gives the bits mpdo_sample
+ * gives with seeds[s] on a copy of the chain rotated by mpdo_apply_1q.  The
+ * right environments are built once for all schemes (a basis change on a
+ * traced leg leaves it unchanged). */
+mpdo_status mpdo_sample_schemes(mpdo_chain_t ch, const int *order, int L, const int *schemes, int S,
+                                int64_t shots, const uint64_t *seeds, double pfloor, const double *rot,
+                                int8_t *bits_out);
 
 /* ---- Batched evolution of independent circuits ----------------------------
  * A batch runner owns `workers` host threads, each with its own engine (its

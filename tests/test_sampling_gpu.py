@@ -90,3 +90,55 @@ def test_reproducible_under_manual_seed(S):
     torch.manual_seed(42)
     b = c.sample(3000, sample_string=False, _require_counts=False)
     assert a == b
+
+
+def _loop_random_sample(c, schemes, shots, reduced):
+    # Circuit.py:448-466 as the reference runs it: one sample() per scheme
+    return [c.sample(shots, orientation=s, reduced=reduced, sample_string=False, _tqdm_disable=True,
+                     _require_counts=False) for s in schemes]
+
+
+@pytest.mark.parametrize('dtype', [torch.complex128, torch.complex64])
+def test_random_sample_equals_the_per_scheme_loop(S, dtype):
+    # one engine call for all schemes gives, scheme by scheme, the bits of the
+    # reference's loop of sample() calls under the same torch seed
+    c = _noisy(S, dtype=dtype)
+    rng = np.random.default_rng(3)
+    schemes = rng.integers(0, 3, size=(12, 5)).tolist() + [[2] * 5, [0] * 5, [1] * 5]
+    torch.manual_seed(5)
+    batched = c.randomSample(schemes, shots_per_scheme=2000, reduced=[2], _tqdm_disable=True)
+    torch.manual_seed(5)
+    loop = _loop_random_sample(c, schemes, 2000, [2])
+    assert len(batched) == len(schemes)
+    same = sum(a == b for a, b in zip(batched, loop))
+    # complex64 probabilities may differ in the last bit between the two
+    # orders of work, which moves a binomial draw in rare cases
+    assert same == len(schemes) if dtype == torch.complex128 else same >= len(schemes) - 1
+
+
+def test_random_sample_distributions(S):
+    c = _noisy(S)
+    schemes = [[0, 1, 2, 0, 1], [1, 1, 0, 2, 2]]
+    shots = 40000
+    torch.manual_seed(9)
+    out = c.randomSample(schemes, shots_per_scheme=shots, reduced=[2], _tqdm_disable=True)
+    from MPDOSimulator.QuantumGates.SingleGates import MeasureX, MeasureY
+    kept = [0, 1, 3, 4, 5]
+    for s, bits in zip(schemes, out):
+        ch = c._chain.clone()
+        for q, b in zip(kept, s):
+            if b < 2:
+                ch.apply_1q(q, c._np((MeasureX if b == 0 else MeasureY)(dtype=c.dtype).tensor))
+        p = np.asarray(ch.probs(kept))
+        _check_freq(np.array(bits), p / p.sum(), shots)
+
+
+def test_random_sample_bool_and_argument_errors(S):
+    c = _noisy(S)
+    out = c.randomSample([[2] * 6], shots_per_scheme=16, _require_bool_result=True, _tqdm_disable=True)
+    assert len(out) == 1 and len(out[0]) == 16 and all(isinstance(x, bool) for x in out[0][0])
+    assert c.randomSample([], shots_per_scheme=4) == []
+    with pytest.raises(ValueError):
+        c.randomSample([[2] * 5], shots_per_scheme=4)
+    with pytest.raises(Exception, match='basis'):
+        c._chain.sample_schemes(list(range(6)), [[3] * 6], 4, [1])

@@ -108,18 +108,18 @@ def test_drop_in_entry_points(mg):
     from MPDOSimulator import TNNOptimizer as T
     c = S.TensorCircuit(5, ideal=False, noiseType='unified', chi=None, kappa=None, dtype=torch.complex128,
                         device='cuda:0')
-    for q in range(5):
-        c.u3(0.3 + q, 0.2 * q, -0.7, [q])
-    for q in range(0, 4, 2):
-        c.cz(q, q + 1)
-    for q in range(1, 4, 2):
-        c.cnot(q, q + 1)
+    for layer in range(4):
+        for q in range(5):
+            c.u3(0.3 + q + layer, 0.2 * q, -0.7, [q])
+        for q in range(layer % 2, 4, 2):
+            c.cz(q, q + 1) if layer % 3 else c.cnot(q, q + 1)
     nodes = c.evolve(S.Tools.create_ket0Series(5, dtype=torch.complex128, connected=True))
     ch = nodes[0]._chain
     rho = ch.reduced_dm()
     T.qr_left2right(nodes)
     _close(ch.reduced_dm(), rho, 'complex128')
+    assert max(d[3] for d in ch.dims()) > 2
     disc = T.svd_right2left(nodes, 2)
-    assert all(d[3] <= 2 for d in ch.dims()) and max(disc) > 0
+    assert all(d[3] <= 2 for d in ch.dims()) and max(disc) > 0 and min(disc) >= 0
     T.svd_left2right(nodes, 2)
     assert all(d[3] <= 2 for d in ch.dims())

@@ -324,11 +324,27 @@ class TensorCircuit(QuantumCircuit):
                      reduced: Optional[List[int]] = None, _tqdm_disable: bool = False,
                      _require_sequential_sample: bool = False, _require_bool_result: bool = False,
                      _stateNodes4Sample=None):
-        """Circuit.py:448-466."""
-        return [self.sample(shots=shots_per_scheme, orientation=s, reduced=reduced, sample_string=False,
-                            _tqdm_disable=True, _require_bool_result=_require_bool_result, _require_counts=False,
-                            _stateNodes4Sample=_stateNodes4Sample)
-                for s in measurement_schemes]
+        """Circuit.py:448-466: ``shots_per_scheme`` samples in each scheme
+        (per measured qubit 0 = X, 1 = Y, 2 = Z), as a list over schemes of
+        bit lists.  All schemes run in one engine call that builds the right
+        environments once; scheme s draws from the seed a ``sample`` call
+        would take at its turn, so the result equals the reference's loop of
+        ``sample`` calls under the same ``torch.manual_seed``."""
+        reduced = reduced or []
+        order = [q for q in range(self.qnumber) if q not in reduced]
+        L = len(order)
+        schemes = [list(s) for s in measurement_schemes]
+        for s in schemes:
+            if len(s) != L:
+                raise ValueError('Length of orientation must match the sample length. Check reduced or unmeasured '
+                                 'qubits.')
+        if not schemes:
+            return []
+        chain = self._sample_source(_stateNodes4Sample)
+        rot = np.stack([self._np(M(dtype=self.dtype, device='cpu').tensor) for M in (MeasureX, MeasureY)])
+        seeds = [int(torch.randint(0, 2 ** 62, (1,)).item()) for _ in schemes]
+        raw = chain.sample_schemes(order, schemes, shots_per_scheme, seeds, rot, GLOBAL_MINIMUM)
+        return [torch.from_numpy(r.astype(np.bool_ if _require_bool_result else np.int32)).tolist() for r in raw]
 
 
 def evolve_batch(circuits: List[TensorCircuit], states: Optional[List[List[QubitNode]]] = None,

@@ -799,7 +799,8 @@ static void discarded_to_host(Engine &e, const DBuf<double> &w, int nb, double *
   std::vector<double> h(2 * (size_t)nb);
   MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), w.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
   MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
-  for (int i = 0; i < nb; ++i) out[i] = h[2 * i + 1] > 0 ? (h[2 * i + 1] - h[2 * i]) / h[2 * i + 1] : 0.0;
+  for (int i = 0; i < nb; ++i)
+    out[i] = h[2 * i + 1] > 0 ? std::max(0.0, (h[2 * i + 1] - h[2 * i]) / h[2 * i + 1]) : 0.0;
 }
 
 // TNNOptimizer.py:111-134: for idx = n-1 .. 1, A_{idx-1} = Q R, Y = R A_idx,
@@ -984,7 +985,8 @@ static void truncate_layer(mpdo_chain_s *ch, int chi, int kappa, double max_err,
       std::vector<double> h(2 * (ch->n - 1));
       MPDO_CUDA_CHECK(cudaMemcpyAsync(h.data(), w.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
       MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
-      for (int i = 0; i < ch->n - 1; ++i) disc_out[i] = h[2 * i + 1] > 0 ? (h[2 * i + 1] - h[2 * i]) / h[2 * i + 1] : 0.0;
+      for (int i = 0; i < ch->n - 1; ++i)
+        disc_out[i] = h[2 * i + 1] > 0 ? std::max(0.0, (h[2 * i + 1] - h[2 * i]) / h[2 * i + 1]) : 0.0;
     } else {
       for (int i = 0; i < ch->n - 1; ++i) disc_out[i] = 0.0;
     }
@@ -1134,25 +1136,37 @@ template <typename T> static double expect_ops(mpdo_chain_s *ch, const int *site
   return (double)h[0].x;
 }
 
-// Circuit.py:297-446 sample: conditional sampling of the qubits `order`
-// (ascending; the other qubits traced), shots split into groups that share a
-// measured prefix.  The right environments (everything to the right traced)
-// do not depend on the prefix and are built once; the left environment of
-// every group advances one site per step in one batched step (mode 2 gives
-// the x = 0 / 1 projections of all groups), and p(x | prefix) is the full
-// contraction with the right environment, plus the floor `pfloor` on both
-// outcomes as in the reference.  Splits draw binomials from a seeded host
-// generator; bit rows of a group's 1-branch come first.
+// Circuit.py:297-466 sample / randomSample: conditional sampling of the
+// qubits `order` (ascending; the other qubits traced) in S measurement
+// schemes at once, shots split into groups that share a scheme and a
+// measured prefix.  Scheme s measures order[j] in basis schemes[s*L + j]
+// (0: X, 1: Y, 2: Z); X and Y rotate the site by the 2 x 2 gate rot[0] or
+// rot[1] first (MeasureX / MeasureY), with the same kernel as a 1q gate.
+// The right environments (everything to the right traced) depend neither on
+// the prefix nor on the scheme -- a unitary on a traced leg leaves the trace
+// unchanged -- and are built once.  The left environment of every group
+// advances one site per step, in one batched step per basis in use (mode 2
+// gives the x = 0 / 1 projections of all groups), and p(x | prefix) is the
+// full contraction with the right environment, plus the floor `pfloor` on
+// both outcomes as in the reference.  Splits draw binomials from one seeded
+// host generator per scheme, groups in order, so scheme s gives the same bits
+// as a single-scheme call with seeds[s]; bit rows of a group's 1-branch come
+// first.  Schemes run in chunks whose group environments fit 2 GiB.
 template <typename T>
-static void sample_chain(mpdo_chain_s *ch, const int *order, int L, int64_t shots, uint64_t seed, double pfloor,
-                         int8_t *out) {
+static void sample_schemes(mpdo_chain_s *ch, const int *order, int L, const int *schemes, int S, int64_t shots,
+                           const uint64_t *seeds, double pfloor, const double *rot, int8_t *out) {
   Engine &e = ch->eng->e;
   check_keep(ch, order, L, ch->n);
-  if (L < 1 || shots < 1) fail(MPDO_ERR_INVALID, "need at least one qubit and one shot");
+  if (L < 1 || shots < 1 || S < 1) fail(MPDO_ERR_INVALID, "need at least one qubit, one shot and one scheme");
+  for (int64_t q = 0; q < (int64_t)S * L; ++q) {
+    if (schemes[q] < 0 || schemes[q] > 2) fail(MPDO_ERR_INVALID, "measurement basis must be 0 (X), 1 (Y) or 2 (Z)");
+    if (schemes[q] < 2 && !rot) fail(MPDO_ERR_INVALID, "X or Y measurement without rotation gates");
+  }
   materialize_all<T>(ch);
   const int n = ch->n;
-  std::memset(out, 0, (size_t)shots * L);
-  // right environments R[k] (l_k x l_k), R[n] = [1]
+  std::memset(out, 0, (size_t)S * shots * L);
+  // right environments R[k] (l_k x l_k), R[n] = [1]; only R[k + 1] of
+  // measured sites k is read
   std::vector<DBuf<cx<T>>> R(n + 1);
   R[n] = DBuf<cx<T>>(e, 1);
   {
@@ -1160,7 +1174,6 @@ static void sample_chain(mpdo_chain_s *ch, const int *order, int L, int64_t shot
     MPDO_CUDA_CHECK(cudaMemcpyAsync(R[n].p, &one, sizeof(one), cudaMemcpyHostToDevice, e.stream));
     MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
   }
-  // (only R[k + 1] of measured sites k is read)
   for (int k = n - 1; k > order[0]; --k) {
     const Site s = ch->s[k];
     const int rows = s.l * 2 * s.a, ar = 2 * s.a * s.r;
@@ -1169,53 +1182,124 @@ static void sample_chain(mpdo_chain_s *ch, const int *order, int L, int64_t shot
     R[k] = DBuf<cx<T>>(e, (size_t)s.l * s.l);
     gemm<T>(e, s.l, s.l, ar, RM<T>(G.p, ar), CM<T>(site_ptr<T>(ch, k), ar, 1), R[k].p, s.l);
   }
-  struct Grp { int64_t start, len; };
-  std::vector<Grp> groups{{0, shots}};
-  std::mt19937_64 rng(seed);
-  Env<T> env = env_start<T>(e);
-  int j = 0;
-  for (int k = 0; k < n && j < L; ++k) {
-    if (order[j] != k) {
-      env_step<T>(e, env, site_ptr<T>(ch, k), ch->s[k], 0, nullptr);
-      continue;
-    }
-    env_step<T>(e, env, site_ptr<T>(ch, k), ch->s[k], 2, nullptr);     // P = 2 G: (group, x)
-    const int G2 = (int)env.P;
-    const int64_t msz = (int64_t)env.r * env.r;
-    DBuf<double> pr(e, G2);
-    env_dot<T>(e.stream, env.E.p, R[k + 1].p, msz, G2, pr.p);
-    std::vector<double> hp(G2);
-    MPDO_CUDA_CHECK(cudaMemcpyAsync(hp.data(), pr.p, G2 * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
-    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
-    std::vector<Grp> next;
-    std::vector<int> parent;
-    for (size_t g = 0; g < groups.size(); ++g) {
-      const double p0 = hp[2 * g] + pfloor, p1 = hp[2 * g + 1] + pfloor;
-      if (!(p0 >= 0) || !(p1 >= 0))
-        fail(MPDO_ERR_NONFINITE, "State is illegal: conditional probabilities " + std::to_string(p0) + ", " +
-                                     std::to_string(p1));
-      const double q = p1 / (p0 + p1);
-      const int64_t len = groups[g].len;
-      int64_t k1;
-      if (q < pfloor) k1 = 0;
-      else if (q > 1 - pfloor) k1 = len;
-      else k1 = std::binomial_distribution<int64_t>(len, q)(rng);
-      for (int64_t r = 0; r < k1; ++r) out[(size_t)(groups[g].start + r) * L + j] = 1;
-      if (k1 > 0) { next.push_back({groups[g].start, k1}); parent.push_back((int)(2 * g + 1)); }
-      if (len - k1 > 0) { next.push_back({groups[g].start + k1, len - k1}); parent.push_back((int)(2 * g)); }
-    }
-    ++j;
-    if (j == L) break;
-    DBuf<int> idx(e, parent.size());
-    MPDO_CUDA_CHECK(cudaMemcpyAsync(idx.p, parent.data(), parent.size() * sizeof(int), cudaMemcpyHostToDevice,
-                                    e.stream));
-    DBuf<cx<T>> En(e, (size_t)parent.size() * msz);
-    gather_mats<T>(e.stream, env.E.p, En.p, idx.p, msz, (int)parent.size());
-    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));   // (idx is pageable host data)
-    env.E = std::move(En);
-    env.P = (int64_t)parent.size();
-    groups.swap(next);
+  // device bytes one group holds at once (environment, the step's
+  // intermediate and its projections) at the widest site
+  double per_group = 1;
+  for (int k = 0; k < n; ++k) {
+    const Site s = ch->s[k];
+    per_group = std::max(per_group, (double)sizeof(cx<T>) *
+                                        ((double)s.l * s.l + 2.0 * s.l * s.a * s.r + 4.0 * s.r * s.r));
   }
+  const double budget = 2.0 * (1 << 30);
+  const double groups_per_scheme = (double)(L >= 62 ? shots : std::min<int64_t>(shots, (int64_t)1 << L));
+  const int chunk = (int)std::max(1.0, std::min((double)S, std::floor(budget / (per_group * groups_per_scheme))));
+
+  struct Grp { int s; int64_t start, len; };
+  for (int s0 = 0; s0 < S; s0 += chunk) {
+    const int s1 = std::min(S, s0 + chunk);
+    std::vector<Grp> groups;
+    std::vector<int> genv;                                   // environment of each group
+    std::vector<std::mt19937_64> rng;
+    for (int s = s0; s < s1; ++s) {
+      groups.push_back({s, (int64_t)s * shots, shots});
+      genv.push_back(0);
+      rng.emplace_back(seeds[s]);
+    }
+    Env<T> env = env_start<T>(e);
+    int j = 0;
+    for (int k = 0; k < n && j < L; ++k) {
+      const Site st = ch->s[k];
+      if (order[j] != k) {
+        env_step<T>(e, env, site_ptr<T>(ch, k), st, 0, nullptr);
+        continue;
+      }
+      const int G = (int)groups.size();
+      std::vector<int> by[3];
+      for (int g = 0; g < G; ++g) by[schemes[(size_t)groups[g].s * L + j]].push_back(g);
+      const int64_t msz = (int64_t)st.r * st.r;
+      const int64_t esz = (int64_t)env.r * env.r;
+      DBuf<cx<T>> proj(e, (size_t)2 * G * msz);              // per group (in basis order): x = 0, 1
+      std::vector<int> pos(G);
+      int off = 0;
+      for (int b = 0; b < 3; ++b) {
+        if (by[b].empty()) continue;
+        const int Gb = (int)by[b].size();
+        Env<T> sub;
+        sub.r = env.r;
+        sub.P = Gb;
+        bool ident = Gb == G && Gb == (int)env.P;   // every group, in environment order
+        for (int i = 0; i < Gb && ident; ++i) ident = genv[by[b][i]] == i;
+        if (ident) {
+          sub.E = std::move(env.E);
+        } else {
+          std::vector<int> src(Gb);
+          for (int i = 0; i < Gb; ++i) src[i] = genv[by[b][i]];
+          DBuf<int> idx(e, Gb);
+          MPDO_CUDA_CHECK(cudaMemcpyAsync(idx.p, src.data(), Gb * sizeof(int), cudaMemcpyHostToDevice, e.stream));
+          sub.E = DBuf<cx<T>>(e, (size_t)Gb * esz);
+          gather_mats<T>(e.stream, env.E.p, sub.E.p, idx.p, esz, Gb);
+          MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));   // (src is pageable host data)
+        }
+        DBuf<cx<T>> Ar;
+        const cx<T> *A = site_ptr<T>(ch, k);
+        if (b < 2) {
+          Ar = DBuf<cx<T>>(e, st.elems());
+          prof(e, K_KRAUS1Q, 8.0 * 2 * 2 * st.elems(), (double)sizeof(cx<T>) * st.elems() * 2,
+               [&] { kraus1q<T>(e.stream, A, Ar.p, st.l, st.a, st.r, rot + 8 * b, 1); });
+          A = Ar.p;
+        }
+        env_step<T>(e, sub, A, st, 2, nullptr);
+        MPDO_CUDA_CHECK(cudaMemcpyAsync(proj.p + (size_t)2 * off * msz, sub.E.p, sizeof(cx<T>) * 2 * Gb * msz,
+                                        cudaMemcpyDeviceToDevice, e.stream));
+        for (int i = 0; i < Gb; ++i) pos[by[b][i]] = off + i;
+        off += Gb;
+      }
+      DBuf<double> pr(e, 2 * G);
+      env_dot<T>(e.stream, proj.p, R[k + 1].p, msz, 2 * G, pr.p);
+      std::vector<double> hp(2 * G);
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(hp.data(), pr.p, 2 * G * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
+      MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+      std::vector<Grp> next;
+      std::vector<int> parent;
+      for (int g = 0; g < G; ++g) {
+        const int pg = pos[g];
+        const double p0 = hp[2 * pg] + pfloor, p1 = hp[2 * pg + 1] + pfloor;
+        if (!(p0 >= 0) || !(p1 >= 0))
+          fail(MPDO_ERR_NONFINITE, "State is illegal: conditional probabilities " + std::to_string(p0) + ", " +
+                                       std::to_string(p1));
+        const double q = p1 / (p0 + p1);
+        const int64_t len = groups[g].len;
+        int64_t k1;
+        if (q < pfloor) k1 = 0;
+        else if (q > 1 - pfloor) k1 = len;
+        else k1 = std::binomial_distribution<int64_t>(len, q)(rng[groups[g].s - s0]);
+        for (int64_t r = 0; r < k1; ++r) out[(size_t)(groups[g].start + r) * L + j] = 1;
+        if (k1 > 0) { next.push_back({groups[g].s, groups[g].start, k1}); parent.push_back(2 * pg + 1); }
+        if (len - k1 > 0) { next.push_back({groups[g].s, groups[g].start + k1, len - k1}); parent.push_back(2 * pg); }
+      }
+      ++j;
+      if (j == L) break;
+      DBuf<int> idx(e, parent.size());
+      MPDO_CUDA_CHECK(cudaMemcpyAsync(idx.p, parent.data(), parent.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                      e.stream));
+      DBuf<cx<T>> En(e, (size_t)parent.size() * msz);
+      gather_mats<T>(e.stream, proj.p, En.p, idx.p, msz, (int)parent.size());
+      MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));   // (parent is pageable host data)
+      env.E = std::move(En);
+      env.P = (int64_t)parent.size();
+      env.r = st.r;
+      groups.swap(next);
+      genv.resize(groups.size());
+      for (size_t g = 0; g < groups.size(); ++g) genv[g] = (int)g;
+    }
+  }
+}
+
+template <typename T>
+static void sample_chain(mpdo_chain_s *ch, const int *order, int L, int64_t shots, uint64_t seed, double pfloor,
+                         int8_t *out) {
+  std::vector<int> z((size_t)std::max(L, 1), 2);
+  sample_schemes<T>(ch, order, L, z.data(), 1, shots, &seed, pfloor, nullptr, out);
 }
 
 // ------------------------------------------------------------ status ----
@@ -1703,6 +1787,16 @@ mpdo_status mpdo_sample(mpdo_chain_t ch, const int *order, int L, int64_t shots,
     set_device(ch->eng);
     if (ch->dtype == MPDO_C64) sample_chain<float>(ch, order, L, shots, seed, pfloor, bits_out);
     else sample_chain<double>(ch, order, L, shots, seed, pfloor, bits_out);
+  });
+}
+
+mpdo_status mpdo_sample_schemes(mpdo_chain_t ch, const int *order, int L, const int *schemes, int S, int64_t shots,
+                                const uint64_t *seeds, double pfloor, const double *rot, int8_t *bits_out) {
+  return guard([&] {
+    need(ch && order && schemes && seeds && bits_out, "NULL argument");
+    set_device(ch->eng);
+    if (ch->dtype == MPDO_C64) sample_schemes<float>(ch, order, L, schemes, S, shots, seeds, pfloor, rot, bits_out);
+    else sample_schemes<double>(ch, order, L, schemes, S, shots, seeds, pfloor, rot, bits_out);
   });
 }
 

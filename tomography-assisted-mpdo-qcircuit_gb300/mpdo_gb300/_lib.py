@@ -72,6 +72,8 @@ SIGNATURES = {
     'mpdo_expect_ops': (_I, [_P, _IP, _DP, _I, _DP]),
     'mpdo_expect_pauli_batch': (_I, [_P, C.POINTER(C.c_int8), _I, _DP]),
     'mpdo_sample': (_I, [_P, _IP, _I, C.c_int64, C.c_uint64, _D, C.POINTER(C.c_int8)]),
+    'mpdo_sample_schemes': (_I, [_P, _IP, _I, _IP, _I, C.c_int64, C.POINTER(C.c_uint64), _D, _DP,
+                                 C.POINTER(C.c_int8)]),
     'mpdo_debug_qr': (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_debug_svd': (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     'mpdo_debug_split': (_I, [_P, _I, _I, _I, _I, _DP, _DP, _DP]),

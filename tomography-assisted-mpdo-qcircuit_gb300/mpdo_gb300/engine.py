@@ -193,6 +193,28 @@ class Chain:
                                     out.ctypes.data_as(C.POINTER(C.c_int8))))
         return out
 
+    def sample_schemes(self, order: Sequence[int], schemes, shots: int, seeds: Sequence[int], rot=None,
+                       pfloor: float = 2.718281828459045e-8) -> np.ndarray:
+        """Conditional sampling in several measurement schemes at once
+        (``schemes``: S x len(order) of 0 = X, 1 = Y, 2 = Z; ``rot``: the X
+        and Y basis-change gates, 2 x 2 x 2 complex): S x shots x len(order)
+        array of 0/1 (int8).  Scheme s equals ``sample`` with ``seeds[s]`` on
+        a copy rotated by those gates."""
+        o = np.ascontiguousarray(np.asarray(order, dtype=np.int32))
+        sc = np.ascontiguousarray(np.asarray(schemes, dtype=np.int32).reshape(-1, len(o)))
+        S = sc.shape[0]
+        sd = np.ascontiguousarray(np.asarray([int(x) & (2 ** 64 - 1) for x in seeds], dtype=np.uint64))
+        if sd.size != S:
+            raise ValueError('one seed per scheme')
+        rb = None if rot is None else _cplx(np.asarray(rot, dtype=np.complex128).reshape(2, 2, 2))
+        out = np.zeros((S, int(shots), len(o)), dtype=np.int8)
+        check(self._lib.mpdo_sample_schemes(self.handle, o.ctypes.data_as(C.POINTER(C.c_int)), len(o),
+                                            sc.ctypes.data_as(C.POINTER(C.c_int)), S, int(shots),
+                                            sd.ctypes.data_as(C.POINTER(C.c_uint64)), float(pfloor),
+                                            None if rb is None else _dptr(rb),
+                                            out.ctypes.data_as(C.POINTER(C.c_int8))))
+        return out
+
     def qr_left2right(self) -> None:
         """TNNOptimizer.py:87-108 on its own."""
         check(self._lib.mpdo_qr_left2right(self.handle))
