@@ -83,6 +83,11 @@ def parse():
     ap.add_argument('--grad-steps', type=int, default=2, help='timed adjoint gradients (0: none)')
     ap.add_argument('--grad-warmup', type=int, default=1)
     ap.add_argument('--no-parity', action='store_true')
+    ap.add_argument('--workload', default='u3_brickwork', choices=['u3_brickwork', 'uneven'],
+                    help='uneven: the 256-circuit uneven batch (one step = the whole batch)')
+    ap.add_argument('--circuits', type=int, default=256, help='uneven: circuits (seeds 0..K-1) over all ranks')
+    ap.add_argument('--sequential', action='store_true',
+                    help='uneven: also run every circuit one at a time through the plain path (long)')
     return ap.parse_args()
 
 
@@ -158,58 +163,10 @@ def program(w, ops, dtype):
 
 # ---------------------------------------------- reference shape trace (8d) --
 def reference_trace_flops(w, K1=8, K2=16):
-    """Flops of the reference's algorithm on this circuit (Circuit.py:74-178,
-    469-491; TNNOptimizer.py:87-197), from its shape trace: per 1q gate the
-    Kraus contraction, per 2q gate the two-site contraction, the gate mix and
-    the thin SVD of theta; per truncate the QR of every site with R absorbed,
-    the thin SVD of every contracted pair of the right-to-left sweep and the
-    kappa SVDs.  Contraction M x N x K: 8 M N K; Householder QR m x n (m >= n):
-    4 (4 m n^2 - 4 n^3 / 3); thin SVD m x n (m >= n): 4 (4 m n^2 + 22 n^3).
-    The split keeps min(rows, cols) values (the reference's cutoff only drops
-    a tail under 2.7e-8).  Host arithmetic only."""
-    def qr(m, n):
-        m, n = max(m, n), min(m, n)
-        return 4.0 * (4.0 * m * n * n - 4.0 * n ** 3 / 3)
-
-    def svd(m, n):
-        m, n = max(m, n), min(m, n)
-        return 4.0 * (4.0 * m * n * n + 22.0 * n ** 3)
-    n = w.n
-    l, a, r = [1] * n, [1] * n, [1] * n
-    total, per_layer, cur = 0.0, [], 0.0
-    for L in w.layers:
-        if L[0] == '1q':
-            q = L[3]
-            cur += 8.0 * 2 * K1 * 2 * l[q] * a[q] * r[q]
-            a[q] *= K1
-        elif L[0] == '2q':
-            i = min(L[3], L[4])
-            m = r[i]
-            rows, cols = l[i] * 2 * a[i], 2 * a[i + 1] * K2 * r[i + 1]
-            cur += 8.0 * rows * (2 * a[i + 1] * r[i + 1]) * m + 8.0 * 4 * K2 * 4 * l[i] * a[i] * a[i + 1] * r[i + 1]
-            cur += svd(rows, cols)
-            keep = min(rows, cols)
-            r[i] = l[i + 1] = keep
-            a[i + 1] *= K2
-        else:
-            for i in range(n - 1):                                   # QR sweep
-                mm, nn = l[i] * 2 * a[i], r[i]
-                k = min(mm, nn)
-                cur += qr(mm, nn) + 8.0 * k * nn * 2 * a[i + 1] * r[i + 1]
-                r[i] = l[i + 1] = k
-            for idx in range(n - 1, 0, -1):                          # SVD sweep on contracted pairs
-                rows, cols = l[idx - 1] * 2 * a[idx - 1], 2 * a[idx] * r[idx]
-                cur += 8.0 * rows * cols * r[idx - 1] + svd(rows, cols)
-                keep = min(w.chi, rows, cols)
-                r[idx - 1] = l[idx] = keep
-            for i in range(n):                                       # kappa pass
-                if a[i] > w.kappa:
-                    cur += svd(l[i] * 2 * r[i], a[i])
-                    a[i] = min(w.kappa, l[i] * 2 * r[i], a[i])
-            per_layer.append(cur)
-            total += cur
-            cur = 0.0
-    return total + cur, per_layer
+    """Flops of the reference's algorithm on this circuit from its shape trace
+    (mpdo_gb300.schedule.reference_flops)."""
+    from mpdo_gb300.schedule import reference_flops
+    return reference_flops(w, K1, K2)
 
 
 # ----------------------------------------------------------------- clocks --
@@ -671,10 +628,114 @@ def gpu_arm(args):
     print(json.dumps(out), flush=True)
 
 
+def uneven_circuits(rank, ws, count):
+    """This rank's circuits of the uneven batch (seeds 0..count-1): the
+    longest-processing-time split of their reference-trace flops over ws
+    ranks.  Returns (seeds, per-rank estimated flops, imbalance)."""
+    from mpdo_gb300.schedule import imbalance, partition, reference_flops
+    from mpdo_gb300.workloads import uneven_batch_circuit
+    costs = [reference_flops(uneven_batch_circuit(s))[0] for s in range(count)]
+    parts = partition(costs, ws)
+    return parts[rank], [sum(costs[i] for i in p) for p in parts], imbalance(parts, costs)
+
+
+def uneven_arm(args):
+    """The uneven batch: circuits with n ~ U{12..40}, depth ~ U{10..30},
+    chi from {16, 32, 64, 128}, kappa from {2, 4} (workloads.uneven_batch_circuit),
+    complex64.  One step evolves this rank's share of them through the batch
+    runner; value = gate layers of all ranks' circuits per second (max time
+    over ranks).  --sequential also runs this rank's circuits one at a time
+    through one engine (the plain path), timed in full, for the ratio."""
+    import torch
+    rank, ws, local = dist_init(args)
+    torch.cuda.set_device(local)
+    import mpdo_gb300
+    mpdo_gb300.build()
+    from mpdo_gb300 import Batch, Engine
+    from mpdo_gb300.workloads import uneven_batch_circuit
+    seeds, rank_flops, imb = uneven_circuits(rank, ws, args.circuits)
+    works = [uneven_batch_circuit(s) for s in seeds]
+    device = f'cuda:{local}'
+    progs = [program(w, host_ops(w, args.dtype, device)[1], args.dtype) for w in works]
+    layers = sum(w.gate_layers for w in works)
+    gates = sum(w.gates for w in works)
+    batch = Batch.get(local, args.workers)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device='cuda')
+    for _ in range(args.warmup):
+        batch.run(progs)
+    torch.cuda.synchronize()
+    barrier(ws)
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            batch.run(progs)
+            b.record()
+            b.synchronize()
+            step_ms.append(a.elapsed_time(b))
+    barrier(ws)
+    clocks = clk.summary()
+    total_ms = allreduce_max(sum(step_ms), ws)
+    all_layers = allreduce_sum(layers, ws)
+    all_gates = allreduce_sum(gates, ws)
+    value = all_layers * args.steps / (total_ms / 1e3)
+    seq = None
+    if args.sequential:
+        eng = Engine.get(local)
+        t_seq = []
+        for w, p in zip(works, progs):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ch = run_chain(p['ops'], w, args.dtype, eng)
+            eng.sync()
+            t_seq.append(time.perf_counter() - t0)
+            del ch
+        seq_s = allreduce_max(sum(t_seq), ws)
+        seq = {'value': all_layers / seq_s, 'unit': 'gate-layers/s', 'seconds': seq_s,
+               'path': 'the same circuits one at a time through one engine (Chain ops), wall clock',
+               'slowest_circuit_s': max(t_seq)}
+    if rank != 0:
+        return
+    chis = {}
+    for w in works:
+        chis[w.chi] = chis.get(w.chi, 0) + 1
+    out = {'metric': 'gate-layers/s, uneven batch (256 circuits)', 'value': value, 'unit': 'gate-layers/s',
+           'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': total_ms / args.steps,
+           'higher_is_better': True, 'scaling': 'strong', 'vs_baseline': None, 'dtype': 'c64',
+           'data': 'synthetic',
+           'config': {'workload': f'uneven batch, seeds 0..{args.circuits - 1}: n ~ U{{12..40}}, depth ~ '
+                                  'U{10..30}, chi in {16, 32, 64, 128}, kappa in {2, 4}, U3 + CZ/CNOT brickwork '
+                                  'with the n=32 workload noise',
+                      'circuits': args.circuits, 'circuits_this_rank': len(works), 'chi_histogram': chis,
+                      'gate_layers': all_layers, 'gates': all_gates, 'workers': batch.workers,
+                      'l2': 'flushed before each step; each step is ~minutes of work',
+                      'partition': {'rule': 'longest processing time first on the reference-trace flops',
+                                    'rank_flops': rank_flops, 'imbalance': imb,
+                                    'measured_on_hardware': ws > 1}},
+           'gates_per_s': all_gates * args.steps / (total_ms / 1e3), 'clocks': clocks,
+           'sequential_plain': seq, 'batched_over_sequential': value / seq['value'] if seq else None}
+    print(json.dumps(out), flush=True)
+
+
+def allreduce_sum(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device='cuda' if dist.get_backend() == 'nccl' else 'cpu')
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         reference_arm(args)
+    elif args.workload == 'uneven':
+        uneven_arm(args)
     else:
         gpu_arm(args)
 

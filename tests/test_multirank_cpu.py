@@ -63,3 +63,37 @@ def test_reference_arm_rank0_only():
     d = json.loads(lines[0][0])
     assert d['impl'] == 'reference' and d['value'] > 0 and d['unit'] == 'gates/s'
     assert d['cpu_baseline']['value'] == d['value'] and d['e2e']['h2d_bytes_per_step'] == 0
+
+
+def test_uneven_batch_cost_balanced_split():
+    # each rank takes its longest-processing-time share of the 256 uneven
+    # circuits (reference-trace flops); the shares are disjoint, cover every
+    # seed, are even to 1 % in estimated work, and sum/max over ranks agree
+    code = ("import sys, json; sys.argv = ['bench.py', '--workload', 'uneven']; import bench; "
+            "args = bench.parse(); rank, ws, local = bench.dist_init(args); "
+            "seeds, flops, imb = bench.uneven_circuits(rank, ws, 256); "
+            "tot = bench.allreduce_sum(len(seeds), ws); m = bench.allreduce_max(10.0 * (rank + 1), ws); "
+            "print(json.dumps({'rank': rank, 'seeds': seeds, 'flops': flops, 'imb': imb, 'tot': tot, 'max': m}))")
+    outs = _launch(['-c', code], _free_port())
+    for rc, _, err in outs:
+        assert rc == 0, err[-2000:]
+    got = [json.loads(o[1].strip().splitlines()[-1]) for o in outs]
+    seeds = [s for g in got for s in g['seeds']]
+    assert sorted(seeds) == list(range(256))
+    assert all(g['tot'] == 256 and g['max'] == 20.0 for g in got)
+    assert got[0]['flops'] == got[1]['flops'] and got[0]['imb'] < 1.01
+    # an equal split of the seed range is less even
+    from mpdo_gb300.schedule import imbalance, reference_flops
+    from mpdo_gb300.workloads import uneven_batch_circuit
+    costs = [reference_flops(uneven_batch_circuit(s))[0] for s in range(256)]
+    assert imbalance([list(range(128)), list(range(128, 256))], costs) > got[0]['imb']
+
+
+def test_partition_rule():
+    from mpdo_gb300.schedule import imbalance, partition
+    costs = [7.0, 5.0, 4.0, 3.0, 3.0, 2.0]
+    parts = partition(costs, 2)
+    assert parts == [[0, 3, 5], [1, 2, 4]] and imbalance(parts, costs) == 1.0
+    assert partition([], 3) == [[], [], []] and partition([1.0], 1) == [[0]]
+    with pytest.raises(ValueError):
+        partition(costs, 0)

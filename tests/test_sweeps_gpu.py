@@ -106,13 +106,15 @@ def test_drop_in_entry_points(mg):
     # sweep sequence bondTruncate = qr_left2right + svd_right2left by hand
     import MPDOSimulator as S
     from MPDOSimulator import TNNOptimizer as T
-    c = S.TensorCircuit(5, ideal=False, noiseType='unified', chi=None, kappa=None, dtype=torch.complex128,
+    # (kappa keeps the Kraus legs at 2: without it they grow 6-fold per layer)
+    c = S.TensorCircuit(5, ideal=False, noiseType='unified', chi=None, kappa=2, dtype=torch.complex128,
                         device='cuda:0')
     for layer in range(4):
         for q in range(5):
             c.u3(0.3 + q + layer, 0.2 * q, -0.7, [q])
         for q in range(layer % 2, 4, 2):
             c.cz(q, q + 1) if layer % 3 else c.cnot(q, q + 1)
+        c.truncate()
     nodes = c.evolve(S.Tools.create_ket0Series(5, dtype=torch.complex128, connected=True))
     ch = nodes[0]._chain
     rho = ch.reduced_dm()

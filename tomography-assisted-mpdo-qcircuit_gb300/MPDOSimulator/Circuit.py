@@ -104,9 +104,13 @@ class TensorCircuit(QuantumCircuit):
         key = None if gate.variational else '2q:' + gate.name
         if key is not None and key in self.noiseTensorDict:
             return self.noiseTensorDict[key]
-        g = gate.tensor
-        t = self._np(torch.einsum('ijklp, klmn -> ijmnp', self.Noise.dpCTensor2.to(g.device),
-                                  g.to(self.Noise.dpCTensor2.dtype)))
+        # einsum('ijklp, klmn -> ijmnp', dpCTensor2, G) on the host: the
+        # composite is a 16 x 16 x K product, smaller than a device round trip
+        dkey = id(self.Noise.dpCTensor2)
+        if getattr(self, '_dpc2_key', None) != dkey:
+            self._dpc2 = self._np(self.Noise.dpCTensor2)
+            self._dpc2_key = dkey
+        t = np.einsum('ijklp,klmn->ijmnp', self._dpc2, self._gate_np(gate).reshape(2, 2, 2, 2))
         if key is not None:
             self.noiseTensorDict[key] = t
         return t

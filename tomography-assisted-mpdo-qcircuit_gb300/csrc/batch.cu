@@ -40,11 +40,15 @@ void ok(mpdo_status s) {
   if (s != MPDO_OK) throw Failure{s};
 }
 
-// Relative cost used to order the queue (longest first): gate count times
-// the square of the bond cap, the size of the factorised matrices' columns.
+// Relative cost used to order the queue (longest first): per truncate, the
+// factorisations of every bond, each of a matrix about 2 kappa chi wide
+// (cubic in that width), plus the gate work between truncates.
 double cost(const mpdo_program &p) {
-  const double chi = p.chi > 0 ? p.chi : 64.0;
-  return (double)p.nops * p.n * chi * chi;
+  const double chi = p.chi > 0 ? p.chi : 64.0, kap = p.kappa > 0 ? p.kappa : 4.0;
+  double ntrunc = 0;
+  for (int k = 0; k < p.nops; ++k) ntrunc += p.op_kind[k] == MPDO_OP_TRUNCATE;
+  const double w = 2.0 * kap * chi;
+  return (ntrunc + 1.0) * p.n * w * w * w + (double)p.nops * w * w;
 }
 
 mpdo_status run_one(mpdo_engine_t eng, const mpdo_program &p, mpdo_chain_t *keep) {

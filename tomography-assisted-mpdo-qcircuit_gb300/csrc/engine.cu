@@ -48,12 +48,12 @@ void set_last_error(const std::string &msg) { g_last_error = msg; }
 // factors, n > ~100 in complex64), chunks of 2n rows factored in global
 // memory (L2 resident), so that the level still splits across CTAs instead of
 // one CTA sweeping all m rows.
-static int tsqr_chunk_rows(int m, int n, size_t esz, size_t cap) {
+static int tsqr_chunk_rows(int m, int n, size_t esz, size_t cap, double ratio) {
   if ((size_t)m * (n + 2) * esz <= cap) return m;
   size_t mcs = cap / ((size_t)(n + 2) * esz);
   mcs = mcs / 32 * 32;
-  if (mcs > (size_t)n) return (int)std::min<size_t>(mcs, (size_t)m);
-  const int g = (2 * n + 31) / 32 * 32;
+  if (mcs > (size_t)n && (double)mcs >= ratio * n) return (int)std::min<size_t>(mcs, (size_t)m);
+  const int g = ((int)std::ceil(std::max(ratio, 2.0) * n) + 31) / 32 * 32;
   return m > g ? g : m;
 }
 
@@ -76,7 +76,7 @@ void qr(Engine &e, int m, int n, const View<T> &in, cx<T> *Q, cx<T> *R) {
     // largest multiple of 32 that fits (with the explicit-Q pass and its two
     // reflector buffers) and exceeds
     // n, so that every level shrinks the stacked R; else one global chunk
-    int mc = tsqr_chunk_rows(curm, n, esz, cap);
+    int mc = tsqr_chunk_rows(curm, n, esz, cap, e.tsqr_ratio);
     const int nch = (curm + mc - 1) / mc;
     Level L;
     L.m = curm; L.mc = mc; L.nch = nch;
@@ -139,7 +139,7 @@ void qr_r_batched(Engine &e, int batch, int m, int n, const View<T> &in, cx<T> *
   View<T> cur = in;
   int curm = m, last_nch = 1;
   while (true) {
-    int mc = tsqr_chunk_rows(curm, n, esz, cap);
+    int mc = tsqr_chunk_rows(curm, n, esz, cap, e.tsqr_ratio);
     const int nch = (curm + mc - 1) / mc;
     v = DBuf<cx<T>>(e, (size_t)batch * nch * mc * n);
     tau = DBuf<cx<T>>(e, (size_t)batch * nch * n);
@@ -193,6 +193,11 @@ static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
   const size_t esz = sizeof(cx<T>), cap = 200 * 1024;
   int bs = (int)std::min<size_t>(cap / (2 * (size_t)m * esz), 32);
   bs = std::max(4, std::min(bs, std::max(8, n / 16)));
+  // a block pair (2 bs columns of m rows) lives in shared memory
+  if (2 * (size_t)bs * m * esz > cap)
+    fail(MPDO_ERR_INVALID, "a wide split of " + std::to_string(m) + " rows exceeds the block-Jacobi shared-memory "
+                           "limit (" + std::to_string(cap / (8 * esz)) + " rows at this precision); truncate the "
+                           "Kraus legs (kappa) or the bonds (chi) before the gate");
   const int nblk = (n + bs - 1) / bs;
   const int nb = nblk + (nblk & 1);
   const int rounds = nb - 1, np = nb / 2;
@@ -1518,6 +1523,10 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
     else if (k == "wide_range_tol") {
       need(value > 0, "wide_range_tol must be positive");
       e.wide_range_tol = value;
+    }
+    else if (k == "tsqr_ratio") {
+      need(value >= 1.0 && value <= 64.0, "tsqr_ratio out of range");
+      e.tsqr_ratio = value;
     }
     else if (k == "wide_oversample") {
       need(value >= 0 && value <= 256, "wide_oversample out of range");

@@ -45,6 +45,10 @@ struct Engine {
   double wide_range_tol = 8.0;      // acceptance: residual <= tol * eps * sqrt(p) * |Y|_F
   int max_sweeps = 60;
   int wide_oversample = 16;          // wide bonds: Rayleigh-Ritz space = leading (want + this) directions
+  // TSQR chunk rows: a shared-memory chunk is used only when it holds at least
+  // tsqr_ratio x n rows, else chunks of ceil(tsqr_ratio n) rows in global memory
+  // (every level shrinks the stack by about that factor)
+  double tsqr_ratio = 1.0;
   int first_status = 0;
   // per-kernel-class profiling (CUDA events around each launch)
   struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };

@@ -339,6 +339,10 @@ cudaError_t hetrd_cluster(cudaStream_t st, int n, const cx<T> *G, T *d, T *e, cx
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaError_t err = cudaLaunchKernelEx(&cfg, k_hetrd<T>, n, G, d, e, vref, tau);
+  if (err != cudaSuccess) {
+    cudaGetLastError();          // not placed: the caller falls back, nothing ran
+    return err;
+  }
   count_launch();
   return err;
 }

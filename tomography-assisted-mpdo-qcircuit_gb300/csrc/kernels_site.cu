@@ -15,6 +15,13 @@ static std::atomic<const char *> g_hist_key[kHistSlots];
 static std::atomic<uint64_t> g_hist_count[kHistSlots];
 
 void count_launch(const char *fn) {
+  // a launch that could not start (shared memory, grid or argument limits)
+  // must not leave its output unwritten silently
+  const cudaError_t err = cudaPeekAtLastError();
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    throw CudaError(err, fn, __FILE__, __LINE__);
+  }
   g_launches.fetch_add(1, std::memory_order_relaxed);
   const uintptr_t h = reinterpret_cast<uintptr_t>(fn);
   for (int i = 0; i < kHistSlots; ++i) {
@@ -54,21 +61,37 @@ inline int nblocks(int64_t n, int t = 256) { return (int)std::min<int64_t>((n + 
 template <typename T> struct Gate1 { cx<T> g[2 * 2 * 16]; };
 template <typename T> struct Gate2 { cx<T> t[16 * 16]; };
 
-template <typename T>
+// V consecutive complex values moved as one access (16 bytes for complex64
+// pairs and single complex128 values)
+template <typename T, int V> struct alignas(sizeof(cx<T>) * V) CVec { cx<T> v[V]; };
+
+// out[l][x][a*K + k][r] = sum_s g[x][s][k] A[l][s][a][r].  Each thread owns
+// V consecutive r of one (l, a): two 16-byte loads, 2 K 16-byte stores, all
+// coalesced across the warp; index arithmetic in I (32-bit unless the output
+// has 2^31 elements or more).
+template <typename T, int V, typename I>
 __global__ void k_kraus1q(const cx<T> *__restrict__ A, cx<T> *__restrict__ out, int L, int Aa, int R, int K,
                           const Gate1<T> G) {
-  const int64_t total = (int64_t)L * Aa * R;
-  const int64_t aK = (int64_t)Aa * K;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t % R, la = t / R, a = la % Aa, l = la / Aa;
-    const cx<T> a0 = A[((l * 2 + 0) * Aa + a) * R + r];
-    const cx<T> a1 = A[((l * 2 + 1) * Aa + a) * R + r];
+  const I Rv = R / V;
+  const I total = (I)L * Aa * Rv;
+  const I aK = (I)Aa * K;
+  for (I t = blockIdx.x * (I)blockDim.x + threadIdx.x; t < total; t += (I)gridDim.x * blockDim.x) {
+    const I rv = t % Rv, la = t / Rv, a = la % Aa, l = la / Aa;
+    const I r = rv * V;
+    const CVec<T, V> a0 = *reinterpret_cast<const CVec<T, V> *>(A + ((l * 2 + 0) * Aa + a) * R + r);
+    const CVec<T, V> a1 = *reinterpret_cast<const CVec<T, V> *>(A + ((l * 2 + 1) * Aa + a) * R + r);
+#pragma unroll
     for (int x = 0; x < 2; ++x) {
       cx<T> *o = out + ((l * 2 + x) * aK + a * K) * R + r;
       for (int k = 0; k < K; ++k) {
-        cx<T> v = cmul<T>(G.g[(x * 2 + 0) * K + k], a0);
-        cfma<T>(v, G.g[(x * 2 + 1) * K + k], a1);
-        o[(int64_t)k * R] = v;
+        const cx<T> g0 = G.g[(x * 2 + 0) * K + k], g1 = G.g[(x * 2 + 1) * K + k];
+        CVec<T, V> v;
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          v.v[q] = cmul<T>(g0, a0.v[q]);
+          cfma<T>(v.v[q], g1, a1.v[q]);
+        }
+        *reinterpret_cast<CVec<T, V> *>(o + (I)k * R) = v;
       }
     }
   }
@@ -304,7 +327,16 @@ template <typename T>
 void kraus1q(cudaStream_t st, const cx<T> *A, cx<T> *out, int L, int Aa, int R, const double *g, int K) {
   Gate1<T> G;
   for (int i = 0; i < 4 * K; ++i) G.g[i] = cmk<T>((T)g[2 * i], (T)g[2 * i + 1]);
-  k_kraus1q<T><<<nblocks((int64_t)L * Aa * R), 256, 0, st>>>(A, out, L, Aa, R, K, G);
+  const int64_t nout = (int64_t)L * 2 * Aa * K * R;
+  const bool pair = sizeof(T) == 4 && R % 2 == 0 && ((uintptr_t)A % 16) == 0 && ((uintptr_t)out % 16) == 0;
+  const int64_t threads = (int64_t)L * Aa * (pair ? R / 2 : R);
+  if (nout < ((int64_t)1 << 31)) {
+    if (pair) k_kraus1q<T, 2, int><<<nblocks(threads), 256, 0, st>>>(A, out, L, Aa, R, K, G);
+    else k_kraus1q<T, 1, int><<<nblocks(threads), 256, 0, st>>>(A, out, L, Aa, R, K, G);
+  } else {
+    if (pair) k_kraus1q<T, 2, int64_t><<<nblocks(threads), 256, 0, st>>>(A, out, L, Aa, R, K, G);
+    else k_kraus1q<T, 1, int64_t><<<nblocks(threads), 256, 0, st>>>(A, out, L, Aa, R, K, G);
+  }
   count_launch();
 }
 
