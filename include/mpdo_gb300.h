@@ -23,6 +23,7 @@
  *   mpdo_expect_ops        dmOperations.py:135-201 expect / pauli_expect
  *                          (single-site operator products)
  *   mpdo_expect_pauli_batch  many pauli_expect terms sharing one pass
+ *   mpdo_trace_rho_rho     dmOperations.py:51-132 trace_rho_rho / purities
  *   mpdo_sample            Circuit.py:297-446 sample (conditional sampling)
  *   mpdo_sample_schemes    Circuit.py:448-466 randomSample (many schemes)
  *
@@ -171,6 +172,12 @@ mpdo_status mpdo_svd_left2right(mpdo_chain_t ch, int chi, double max_err, double
 /* Reduced density matrix on `keep` (m ascending qubit indices; m <= 14):
  * 2^m x 2^m complex, rows = ket (qubit keep[0] most significant). */
 mpdo_status mpdo_reduced_dm(mpdo_chain_t ch, const int *keep, int m, double *host_out);
+/* dmOperations.py:51-66 trace_rho_rho: Re Tr(rho_a rho_b), both states traced
+ * over the qubits not in `keep` (m ascending indices, any m <= n), without
+ * forming either density matrix (four-layer environment sweep; the largest
+ * intermediate holds bond^4 x 2 x Kraus-leg elements).  a and b may be the
+ * same chain; they need the same n and precision. */
+mpdo_status mpdo_trace_rho_rho(mpdo_chain_t a, mpdo_chain_t b, const int *keep, int m, double *out);
 /* Diagonal of the reduced density matrix (real parts), 2^m doubles (m <= 24). */
 mpdo_status mpdo_probs(mpdo_chain_t ch, const int *keep, int m, double *host_out);
 /* Re Tr(rho . prod_j O_j): ops is m x (2x2 complex) [row][col], on distinct

@@ -631,6 +631,29 @@ def expect_dense(st: MPDO, obs: torch.Tensor, oq: Sequence[int]) -> torch.Tensor
 _PROJ = [torch.tensor([[1, 0], [0, 0]], dtype=torch.complex128), torch.tensor([[0, 0], [0, 1]], dtype=torch.complex128)]
 
 
+def trace_rho_rho(st0: MPDO, st1: MPDO, keep: Sequence[int]) -> float:
+    """dmOperations.py:51-66: Tr(rho_0 rho_1) with both states traced over
+    the qubits not in ``keep`` -- the doubled network contracted site by site
+    (the reference lets tn.contractors.auto pick the order; the value does
+    not depend on it): a kept qubit joins rho_0's ket with rho_1's bra and
+    rho_0's bra with rho_1's ket, a traced one ket with bra in each state."""
+    keep = set(int(q) for q in keep)
+    E = torch.ones(1, 1, 1, 1, dtype=st0.sites[0].dtype)
+    for k in range(st0.n):
+        a0, a1 = st0.sites[k], st1.sites[k]
+        if k in keep:
+            E = torch.einsum('pqst,pxaP->qstxaP', E, a0)
+            E = torch.einsum('qstxaP,qyaQ->stxyPQ', E, a0.conj())
+            E = torch.einsum('stxyPQ,sybS->txPQbS', E, a1)
+            E = torch.einsum('txPQbS,txbT->PQST', E, a1.conj())
+        else:
+            E = torch.einsum('pqst,pxaP->qstxaP', E, a0)
+            E = torch.einsum('qstxaP,qxaQ->stPQ', E, a0.conj())
+            E = torch.einsum('stPQ,szbS->tPQzbS', E, a1)
+            E = torch.einsum('tPQzbS,tzbT->PQST', E, a1.conj())
+    return float(E.reshape(()).real)
+
+
 def conditional_p1(st: MPDO, order: Sequence[int], history: Sequence[int]) -> float:
     """Circuit.py:297-332: the probability that qubit ``order[len(history)]``
     reads 1 given that ``order[:len(history)]`` read ``history``, every other

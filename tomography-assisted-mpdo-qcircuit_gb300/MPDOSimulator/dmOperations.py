@@ -52,13 +52,18 @@ def trace_rho(dmNodes: DMNodes) -> Tensor:
 
 
 def trace_rho_rho(dmNodes_0: DMNodes, dmNodes_1: Optional[DMNodes] = None) -> Tensor:
-    """dmOperations.py:51-66: Tr(rho_0 rho_1) over the untraced qubits."""
+    """dmOperations.py:51-66: Tr(rho_0 rho_1) over the untraced qubits (up to
+    12 of them through the reduced density matrices, beyond that by the
+    engine's four-layer environment sweep)."""
     d1 = dmNodes_1 if dmNodes_1 is not None else dmNodes_0
     if d1.qnumber != dmNodes_0.qnumber:
         raise ValueError('Density matrices must have the same number of nodes.')
     keep = dmNodes_0.kept()
+    if d1.kept() != keep:
+        raise ValueError('Density matrices should have the same untraced qubits.')
     if len(keep) > 12:
-        raise NotImplementedError('Tr(rho rho) over more than 12 untraced qubits')
+        # four-layer environment sweep on the GPU, no density matrix formed
+        return torch.tensor(dmNodes_0.chain.trace_rho_rho(d1.chain, keep), dtype=torch.float64)
     r0 = dmNodes_0.chain.reduced_dm(keep)
     r1 = d1.chain.reduced_dm(keep)
     return torch.tensor(_trace_product(r0, r1), dtype=torch.float64)
@@ -77,8 +82,14 @@ def trace_composited_rho2(*dmNodes: DMNodes) -> Tensor:
     """dmOperations.py:90-132: Tr[(sum_i rho_i)^2] / slices^2."""
     n = len(dmNodes)
     keep = dmNodes[0].kept()
+    if any(d.kept() != keep for d in dmNodes):
+        raise ValueError('Density matrices should have same number of un-traced nodes.')
     if len(keep) > 12:
-        raise NotImplementedError('composite purity over more than 12 untraced qubits')
+        # as the reference beyond 12 qubits: diagonal terms plus twice the cross terms
+        diag = sum(d.chain.trace_rho_rho(d.chain, keep) for d in dmNodes)
+        cross = sum(dmNodes[i].chain.trace_rho_rho(dmNodes[k].chain, keep)
+                    for i in range(n) for k in range(i + 1, n))
+        return torch.tensor((diag + 2 * cross) / n ** 2, dtype=torch.float64)
     rho = sum(d.chain.reduced_dm(keep) for d in dmNodes)
     return torch.tensor(_trace_product(rho, rho) / n ** 2, dtype=torch.float64)
 

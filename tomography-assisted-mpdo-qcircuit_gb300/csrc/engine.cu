@@ -1141,6 +1141,107 @@ template <typename T> static double expect_ops(mpdo_chain_s *ch, const int *site
   return (double)h[0].x;
 }
 
+// dmOperations.py:51-66 trace_rho_rho: Tr(rho_0 rho_1), both states traced
+// over the qubits not in `keep` (ascending), for any number of kept qubits.
+// A left-to-right sweep of the four-layer environment E[p][q][s][t] (ket and
+// bra bonds of rho_0, ket and bra bonds of rho_1): per site four GEMMs, each
+// contracting one layer, with strided permutations between them.  A kept
+// qubit joins rho_0's ket leg with rho_1's bra leg and rho_0's bra leg with
+// rho_1's ket leg; a traced qubit joins ket and bra within each state.  The
+// largest intermediate holds bond^3 x 2 x Kraus x bond elements.
+template <typename T>
+static double trace_rho_rho(mpdo_chain_s *c0, mpdo_chain_s *c1, const int *keep, int m) {
+  Engine &e = c0->eng->e;
+  check_keep(c0, keep, m, c0->n);
+  materialize_all<T>(c0);
+  if (c1 != c0) {
+    materialize_all<T>(c1);
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(c1->eng->e.stream));   // its sites are read on c0's stream
+  }
+  const int n = c0->n;
+  DBuf<cx<T>> E(e, 1);
+  {
+    const cx<T> one = cmk<T>(T(1), T(0));
+    MPDO_CUDA_CHECK(cudaMemcpyAsync(E.p, &one, sizeof(one), cudaMemcpyHostToDevice, e.stream));
+    MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  }
+  int64_t p = 1, s = 1;   // E[p][q = p][s][t = s]
+  auto perm = [&](int64_t elems, const cx<T> *src, std::initializer_list<int64_t> d,
+                  std::initializer_list<int64_t> st) {
+    DBuf<cx<T>> out(e, (size_t)elems);
+    permute<T>(e.stream, out.p, src, (int)d.size(), d.begin(), st.begin(), 0);
+    return out;
+  };
+  int j = 0;
+  for (int k = 0; k < n; ++k) {
+    const bool kept = j < m && keep[j] == k;
+    if (kept) ++j;
+    const Site S0 = c0->s[k], S1 = c1->s[k];
+    if (S0.l != p || S1.l != s) fail(MPDO_ERR_BAD_SHAPE, "bond mismatch in readout");
+    const cx<T> *A0 = site_ptr<T>(c0, k), *A1 = site_ptr<T>(c1, k);
+    const int64_t q = p, t = s, a = S0.a, P = S0.r, b = S1.a, R = S1.r;
+    // F1[q s t][x a P] = sum_p E[p][q s t] A0[p][x a P]
+    const int64_t qst = q * s * t, xaP = 2 * a * P;
+    DBuf<cx<T>> F1(e, (size_t)(qst * xaP));
+    gemm<T>(e, (int)qst, (int)xaP, (int)p, CM<T>(E.p, qst), RM<T>(A0, xaP), F1.p, xaP);
+    E.reset();
+    DBuf<cx<T>> En(e, (size_t)(P * P * R * R));
+    if (kept) {
+      // F2[q s a P][b T] = sum_{t x} F1[q s a P][t x] conj(A1)[t x][b T]
+      DBuf<cx<T>> G = perm(qst * xaP, F1.p, {q, s, a, P, t, 2}, {s * t * xaP, t * xaP, P, 1, xaP, a * P});
+      F1.reset();
+      DBuf<cx<T>> F2(e, (size_t)(q * s * a * P * b * R));
+      gemm<T>(e, (int)(q * s * a * P), (int)(b * R), (int)(2 * t), RM<T>(G.p, 2 * t), RM<T>(A1, b * R, 1), F2.p,
+              b * R);
+      G.reset();
+      // F4[q a P T][y S] = sum_{s b} F2[q a P T][s b] A1[s b][y S]
+      DBuf<cx<T>> F3 = perm(q * s * a * P * b * R, F2.p, {q, a, P, R, s, b},
+                            {s * a * P * b * R, P * b * R, b * R, 1, a * P * b * R, R});
+      F2.reset();
+      DBuf<cx<T>> A1p = perm(s * 2 * b * R, A1, {s, b, 2, R}, {2 * b * R, R, b * R, 1});
+      DBuf<cx<T>> F4(e, (size_t)(q * a * P * R * 2 * R));
+      gemm<T>(e, (int)(q * a * P * R), (int)(2 * R), (int)(s * b), RM<T>(F3.p, s * b), RM<T>(A1p.p, 2 * R), F4.p,
+              2 * R);
+      F3.reset();
+      // F6[P T S][Q] = sum_{q y a} F4[P T S][q y a] conj(A0)[q y a][Q]
+      DBuf<cx<T>> F5 = perm(q * a * P * R * 2 * R, F4.p, {P, R, R, q, 2, a},
+                            {R * 2 * R, 2 * R, 1, a * P * R * 2 * R, R, P * R * 2 * R});
+      F4.reset();
+      DBuf<cx<T>> F6(e, (size_t)(P * R * R * P));
+      gemm<T>(e, (int)(P * R * R), (int)P, (int)(q * 2 * a), RM<T>(F5.p, q * 2 * a), RM<T>(A0, P, 1), F6.p, P);
+      F5.reset();
+      // E[P][Q][S][T] from F6[P][T][S][Q]
+      const int64_t d[4] = {P, P, R, R}, st[4] = {R * R * P, 1, P, R * P};
+      copy4d<T>(e.stream, En.p, F6.p, d, st, 0);
+    } else {
+      // G2[s t P][Q] = sum_{q x a} F1[s t P][q x a] conj(A0)[q x a][Q]
+      DBuf<cx<T>> G1 = perm(qst * xaP, F1.p, {s, t, P, q, 2, a}, {t * xaP, xaP, 1, s * t * xaP, a * P, P});
+      F1.reset();
+      DBuf<cx<T>> G2(e, (size_t)(s * t * P * P));
+      gemm<T>(e, (int)(s * t * P), (int)P, (int)(q * 2 * a), RM<T>(G1.p, q * 2 * a), RM<T>(A0, P, 1), G2.p, P);
+      G1.reset();
+      // G4[t P Q][z b S] = sum_s G2[t P Q][s] A1[s][z b S]
+      DBuf<cx<T>> G3 = perm(s * t * P * P, G2.p, {t, P, P, s}, {P * P, P, 1, t * P * P});
+      G2.reset();
+      const int64_t zbS = 2 * b * R;
+      DBuf<cx<T>> G4(e, (size_t)(t * P * P * zbS));
+      gemm<T>(e, (int)(t * P * P), (int)zbS, (int)s, RM<T>(G3.p, s), RM<T>(A1, zbS), G4.p, zbS);
+      G3.reset();
+      // E[P Q S][T] = sum_{t z b} G4[P Q S][t z b] conj(A1)[t z b][T]
+      DBuf<cx<T>> G5 = perm(t * P * P * zbS, G4.p, {P, P, R, t, 2, b}, {P * zbS, zbS, 1, P * P * zbS, b * R, R});
+      G4.reset();
+      gemm<T>(e, (int)(P * P * R), (int)R, (int)(t * 2 * b), RM<T>(G5.p, t * 2 * b), RM<T>(A1, R, 1), En.p, R);
+    }
+    E = std::move(En);
+    p = P;
+    s = R;
+  }
+  cx<T> h;
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(&h, E.p, sizeof(h), cudaMemcpyDeviceToHost, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  return (double)h.x;
+}
+
 // Circuit.py:297-466 sample / randomSample: conditional sampling of the
 // qubits `order` (ascending; the other qubits traced) in S measurement
 // schemes at once, shots split into groups that share a scheme and a
@@ -1769,6 +1870,15 @@ mpdo_status mpdo_reduced_dm(mpdo_chain_t ch, const int *keep, int m, double *hos
     need(ch && host_out && (keep || m == 0), "NULL argument");
     set_device(ch->eng);
     DISPATCH(ch, reduced_dm, ch, keep, m, host_out);
+  });
+}
+
+mpdo_status mpdo_trace_rho_rho(mpdo_chain_t a, mpdo_chain_t b, const int *keep, int m, double *out) {
+  return guard([&] {
+    need(a && b && out && (keep || m == 0), "NULL argument");
+    need(a->n == b->n && a->dtype == b->dtype, "the two states need the same qubit count and precision");
+    set_device(a->eng);
+    *out = a->dtype == MPDO_C64 ? trace_rho_rho<float>(a, b, keep, m) : trace_rho_rho<double>(a, b, keep, m);
   });
 }
 

@@ -79,6 +79,11 @@ template <typename T>
 void copy4d(cudaStream_t st, cx<T> *dst, const cx<T> *src, const int64_t dims[4], const int64_t sstr[4],
             int conj);
 
+// Strided permutation of up to 6 axes: dst (contiguous, axis order of d) =
+// conj?(src[sum_k i_k s[k]]), nd <= 6 axes
+template <typename T>
+void permute(cudaStream_t st, cx<T> *dst, const cx<T> *src, int nd, const int64_t *d, const int64_t *s, int conj);
+
 // X[i][j] *= f(s[j]) (col scaling) or f(s[i]) (row scaling) for a row-major
 // M x N matrix with leading dimension ld.  mode: 0 = s, 1 = sqrt(s),
 // 2 = 1/sqrt(s), 3 = 1/s; modes 2 and 3 give 0 where s <= rel * s[0]

@@ -146,6 +146,27 @@ __global__ void k_copy4d(cx<T> *dst, const cx<T> *src, int64_t d0, int64_t d1, i
   }
 }
 
+struct Perm6 { int64_t d[6], s[6]; };
+
+// dst (contiguous in the order of d) = conj?(src at sum_k i_k s[k]); unused
+// leading axes have d = 1
+template <typename T>
+__global__ void k_permute6(cx<T> *__restrict__ dst, const cx<T> *__restrict__ src, int64_t total, Perm6 P,
+                           int conj) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t, off = 0;
+#pragma unroll
+    for (int k = 5; k >= 0; --k) {
+      const int64_t i = r % P.d[k];
+      r /= P.d[k];
+      off += i * P.s[k];
+    }
+    cx<T> v = src[off];
+    if (conj) v.y = -v.y;
+    dst[t] = v;
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ T scale_of(T s, int mode, T thr) {
   switch (mode) {
@@ -366,6 +387,21 @@ void copy4d(cudaStream_t st, cx<T> *dst, const cx<T> *src, const int64_t d[4], c
 }
 
 template <typename T>
+void permute(cudaStream_t st, cx<T> *dst, const cx<T> *src, int nd, const int64_t *d, const int64_t *s, int conj) {
+  Perm6 P;
+  int64_t total = 1;
+  for (int k = 0; k < 6; ++k) {
+    const int j = k - (6 - nd);
+    P.d[k] = j >= 0 ? d[j] : 1;
+    P.s[k] = j >= 0 ? s[j] : 0;
+    total *= P.d[k];
+  }
+  if (total <= 0) return;
+  k_permute6<T><<<nblocks(total), 256, 0, st>>>(dst, src, total, P, conj);
+  count_launch();
+}
+
+template <typename T>
 void scale_matrix(cudaStream_t st, cx<T> *X, int M, int N, int64_t ld, const T *s, int by_row, int mode) {
   if ((int64_t)M * N <= 0) return;
   const T thr_rel = sizeof(T) == 4 ? T(1e-6) : T(1e-14);
@@ -431,6 +467,7 @@ void sumsq(cudaStream_t st, const cx<T> *x, size_t n, double *out) {
   template void mix2q_batched<T>(cudaStream_t, const cx<T> *, cx<T> *, int, int, int, int, const double *, \
                                  int);                                                                      \
   template void copy4d<T>(cudaStream_t, cx<T> *, const cx<T> *, const int64_t *, const int64_t *, int);     \
+  template void permute<T>(cudaStream_t, cx<T> *, const cx<T> *, int, const int64_t *, const int64_t *, int); \
   template void scale_matrix<T>(cudaStream_t, cx<T> *, int, int, int64_t, const T *, int, int);             \
   template void blockdiag2<T>(cudaStream_t, cx<T> *, const cx<T> *, int, int, int);                        \
   template void fill_zero<T>(cudaStream_t, cx<T> *, size_t);                                               \

@@ -68,6 +68,7 @@ SIGNATURES = {
     'mpdo_svd_right2left': (_I, [_P, _I, _D, _DP]),
     'mpdo_svd_left2right': (_I, [_P, _I, _D, _DP]),
     'mpdo_reduced_dm': (_I, [_P, _IP, _I, _DP]),
+    'mpdo_trace_rho_rho': (_I, [_P, _P, _IP, _I, _DP]),
     'mpdo_probs': (_I, [_P, _IP, _I, _DP]),
     'mpdo_expect_ops': (_I, [_P, _IP, _DP, _I, _DP]),
     'mpdo_expect_pauli_batch': (_I, [_P, C.POINTER(C.c_int8), _I, _DP]),

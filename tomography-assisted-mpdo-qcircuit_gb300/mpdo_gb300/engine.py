@@ -266,6 +266,16 @@ class Chain:
         check(self._lib.mpdo_reduced_dm(self.handle, arr, m, _dptr(out)))
         return out.view(np.complex128).reshape(2 ** m, 2 ** m)
 
+    def trace_rho_rho(self, other: Optional['Chain'] = None, keep: Optional[Sequence[int]] = None) -> float:
+        """Re Tr(rho_self rho_other) with both states traced over the qubits
+        not in ``keep`` (default: all kept), for any number of kept qubits."""
+        other = self if other is None else other
+        keep = list(range(self.n)) if keep is None else sorted(int(q) for q in keep)
+        arr = (C.c_int * max(len(keep), 1))(*keep)
+        out = C.c_double()
+        check(self._lib.mpdo_trace_rho_rho(self.handle, other.handle, arr, len(keep), C.byref(out)))
+        return out.value
+
     def probs(self, keep: Optional[Sequence[int]] = None) -> np.ndarray:
         keep = list(range(self.n)) if keep is None else sorted(int(q) for q in keep)
         m = len(keep)
