@@ -83,6 +83,8 @@ def parse():
     ap.add_argument('--grad-steps', type=int, default=2, help='timed adjoint gradients (0: none)')
     ap.add_argument('--grad-warmup', type=int, default=1)
     ap.add_argument('--no-parity', action='store_true')
+    ap.add_argument('--autotune', action='store_true',
+                    help='apply the autotuner\'s cached options for this class (tuning first when none are cached)')
     ap.add_argument('--workload', default='u3_brickwork', choices=['u3_brickwork', 'uneven'],
                     help='uneven: the 256-circuit uneven batch (one step = the whole batch)')
     ap.add_argument('--circuits', type=int, default=256, help='uneven: circuits (seeds 0..K-1) over all ranks')
@@ -474,6 +476,20 @@ def gpu_arm(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
 
+    # ---- engine options: built-in defaults, or the autotuner's for this class
+    tuning = {'source': 'defaults'}
+    if args.autotune:
+        from mpdo_gb300 import autotune
+        opts = autotune.options_for(w.chi, w.kappa, args.dtype, local)
+        tuning = {'source': 'cache', 'options': opts}
+        if not opts:
+            ent = autotune.tune(w.chi, w.kappa, args.dtype, local)
+            opts = ent['options']
+            tuning = {'source': 'tuned before the run', 'options': opts, 'seconds': ent['seconds'],
+                      'default_seconds': ent['default_seconds']}
+        autotune.apply(Engine.get(local), opts)
+        autotune.apply(Batch.get(local, args.workers), opts)
+
     # ---- plain path: one circuit through one engine (device-resident inputs)
     eng = Engine.get(local)
     eng.set_stream(stream.cuda_stream)
@@ -599,6 +615,7 @@ def gpu_arm(args):
                       'workers': batch.workers, 'gates_per_circuit': gates_per_circuit,
                       'gate_layers_per_circuit': w.gate_layers, 'parallelism': f'replicas{ws}',
                       'l2': 'flushed between steps (256 MB write); the per-circuit state is ~8 MB',
+                      'engine_options': tuning,
                       'timing': 'CUDA events on an idle stream around the synchronous batch call'},
            'e2e': {'value': e2e_value, 'unit': 'gates/s', 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': d2h,
                    'ms_per_step': e2e_total / len(e2e_ms),

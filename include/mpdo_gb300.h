@@ -73,6 +73,11 @@ mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
  *   "fuse_2q"    1 (default): a 2q gate followed by truncate() is fused into
  *                the QR sweep; 0: always split theta by SVD first (the
  *                reference's exact sequence, including its split cutoff).
+ *   "defer_1q"   1 (default): a trace-preserving 1q Kraus map (sum K^H K = I)
+ *                is kept pending on its site (composed with later ones while
+ *                K <= 16) and applied when the site is next read; a truncate
+ *                sweeps the pre-gate sites, which gives the same R factors and
+ *                left singular vectors.  0: applied at once.
  *   "wide_range" on bonds too wide for one CTA, first try a verified
  *                randomized range finder (accepted only when the residual
  *                outside its span is at rounding level, so the triplets are
@@ -83,9 +88,17 @@ mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
  *   "wide_eig"   the exact wide-bond path diagonalises the Gram matrix by
  *                Householder tridiagonalisation on a thread-block cluster +
  *                bisection / inverse iteration (1), or by block Jacobi (0);
- *                -1 (default): tridiagonal for complex128, block Jacobi for
- *                complex64.  Both are followed by a Rayleigh-Ritz refinement
- *                in the leading (want + wide_oversample) directions.
+ *                -1 (default): tridiagonal for complex128; in complex64
+ *                block Jacobi below "wide_eig_from" columns (default 257)
+ *                and tridiagonal from there.  Both are followed by a
+ *                Rayleigh-Ritz refinement in the leading
+ *                (want + wide_oversample) directions.
+ *   "bjacobi_bs" block width (columns per block) of the wide-bond block
+ *                Jacobi, capped by shared memory; 0 (default) picks
+ *                max(8, n / 16) up to 32.
+ *   "tsqr_ratio" TSQR chunks hold at least this many times the column count
+ *                in rows (shared memory when they fit, else global memory);
+ *                default 3, so every level shrinks the stacked R threefold.
  *   "wide_oversample" extra Rayleigh-Ritz directions of a wide bond beyond
  *                the kept count (default 16).
  *   "max_sweeps" Jacobi sweep limit (default 60). */

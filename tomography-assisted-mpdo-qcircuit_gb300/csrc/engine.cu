@@ -192,7 +192,7 @@ template <typename T>
 static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
   const size_t esz = sizeof(cx<T>), cap = 200 * 1024;
   int bs = (int)std::min<size_t>(cap / (2 * (size_t)m * esz), 32);
-  bs = std::max(4, std::min(bs, std::max(8, n / 16)));
+  bs = e.bjacobi_bs > 0 ? std::max(4, std::min(bs, e.bjacobi_bs)) : std::max(4, std::min(bs, std::max(8, n / 16)));
   // a block pair (2 bs columns of m rows) lives in shared memory
   if (2 * (size_t)bs * m * esz > cap)
     fail(MPDO_ERR_INVALID, "a wide split of " + std::to_string(m) + " rows exceeds the block-Jacobi shared-memory "
@@ -255,15 +255,17 @@ static void left_svd_wide_exact(Engine &e, const cx<T> *Y, int Mr, int Nc, int w
   DBuf<T> lam, tail;
   bool have = false;
   // Default: tridiagonal for complex128 (1.8x faster than block Jacobi,
-  // both at the oracle to 1e-14), block Jacobi for complex64.  Measured in
-  // complex64 on the n=32, chi=64, kappa=4 circuit against the complex128
-  // oracle: with the error rule 1e-6 (well conditioned) both reach ~2e-5,
-  // the floor that single-precision storage of the state sets there; on the
-  // chi-capped benchmark form (ill-conditioned: complex128 runs that differ
-  // only in rounding spread by 3e-3 at depth 8) Jacobi lands inside the
-  // spread and the tridiagonal route at twice it.  Jacobi also remains where
-  // the cluster does not fit or cannot be placed.
-  const bool use_eig = e.wide_eig > 0 || (e.wide_eig < 0 && sizeof(T) == 8);
+  // both at the oracle to 1e-14); in complex64 block Jacobi up to Grams of
+  // 256 (chi <= 64 at kappa 4) and tridiagonal from wide_eig_from = 257.
+  // Measured in complex64 on the n=32, chi=64, kappa=4 circuit against the
+  // complex128 oracle: with the error rule 1e-6 (well conditioned) both reach
+  // ~2e-5, the floor that single-precision storage of the state sets there;
+  // on the chi-capped benchmark form (ill-conditioned: complex128 runs that
+  // differ only in rounding spread by 3e-3 at depth 8) Jacobi lands inside
+  // the spread and the tridiagonal route at twice it.  On 512-wide Grams
+  // (chi = 128) the Jacobi rounds cost 8x the tridiagonal route.  Jacobi also
+  // remains where the cluster does not fit or cannot be placed.
+  const bool use_eig = e.wide_eig > 0 || (e.wide_eig < 0 && (sizeof(T) == 8 || Mr >= e.wide_eig_from));
   if (use_eig && hetrd_cluster_fits<T>(Mr)) {
     DBuf<T> dd(e, Mr), ee(e, Mr), work(e, (size_t)kr * 2 * Mr);
     DBuf<cx<T>> vref(e, (size_t)(Mr - 1) * (Mr - 1)), tau(e, Mr), Zt(e, (size_t)Mr * kr);
@@ -1621,9 +1623,17 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
     else if (k == "defer_1q") e.defer_1q = value != 0;
     else if (k == "wide_range") e.wide_range = value > 0 ? 1 : (value < 0 ? -1 : 0);
     else if (k == "wide_eig") e.wide_eig = value > 0 ? 1 : (value < 0 ? -1 : 0);
+    else if (k == "wide_eig_from") {
+      need(value >= 2 && value <= 1e9, "wide_eig_from out of range");
+      e.wide_eig_from = (int)value;
+    }
     else if (k == "wide_range_tol") {
       need(value > 0, "wide_range_tol must be positive");
       e.wide_range_tol = value;
+    }
+    else if (k == "bjacobi_bs") {
+      need(value >= 0 && value <= 64, "bjacobi_bs out of range");
+      e.bjacobi_bs = (int)value;
     }
     else if (k == "tsqr_ratio") {
       need(value >= 1.0 && value <= 64.0, "tsqr_ratio out of range");

@@ -39,6 +39,7 @@ struct Engine {
   bool defer_1q = true;              // trace-preserving 1q channels deferred past the truncate sweeps
   int wide_range = -1;              // verified range finder on wide bonds: 1 on, 0 off, -1 complex128 only
   int wide_eig = -1;                // wide-bond Gram: tridiagonal (1), block Jacobi (0), -1: by precision
+  int wide_eig_from = 257;          // (-1, complex64) Grams at least this wide take the tridiagonal route
   long long wide_eig_calls = 0;
   long long wide_range_hits = 0, wide_exact_calls = 0;
   double wide_resid_max = 0;        // largest accepted |Y - Q Q^H Y|_F / |Y|_F
@@ -48,7 +49,8 @@ struct Engine {
   // TSQR chunk rows: a shared-memory chunk is used only when it holds at least
   // tsqr_ratio x n rows, else chunks of ceil(tsqr_ratio n) rows in global memory
   // (every level shrinks the stack by about that factor)
-  double tsqr_ratio = 1.0;
+  double tsqr_ratio = 3.0;
+  int bjacobi_bs = 0;               // block-Jacobi block width (columns); 0: from the shared-memory cap
   int first_status = 0;
   // per-kernel-class profiling (CUDA events around each launch)
   struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };
