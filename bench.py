@@ -678,8 +678,12 @@ def uneven_arm(args):
     gates = sum(w.gates for w in works)
     batch = Batch.get(local, args.workers)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device='cuda')
+    # warm-up: --warmup whole batches, or with --warmup 0 the 16 costliest
+    # circuits once (each step is minutes of work)
     for _ in range(args.warmup):
         batch.run(progs)
+    if args.warmup == 0:
+        batch.run(progs[:16])
     torch.cuda.synchronize()
     barrier(ws)
     step_ms = []
@@ -733,6 +737,7 @@ def uneven_arm(args):
                                     'rank_flops': rank_flops, 'imbalance': imb,
                                     'measured_on_hardware': ws > 1}},
            'gates_per_s': all_gates * args.steps / (total_ms / 1e3), 'clocks': clocks,
+           'warmup_rule': 'whole batches' if args.warmup else 'the 16 costliest circuits once',
            'sequential_plain': seq, 'batched_over_sequential': value / seq['value'] if seq else None}
     print(json.dumps(out), flush=True)
 
