@@ -97,3 +97,59 @@ def test_partition_rule():
     assert partition([], 3) == [[], [], []] and partition([1.0], 1) == [[0]]
     with pytest.raises(ValueError):
         partition(costs, 0)
+
+
+_FIT_CODE = r'''
+import json, os, sys
+import torch
+import torch.distributed as dist
+ROOT = os.getcwd()
+sys.path[:0] = [ROOT, os.path.join(ROOT, 'tomography-assisted-mpdo-qcircuit_gb300'), os.path.join(ROOT, 'tests')]
+from test_multirank_cpu import fit_problem
+dist.init_process_group('gloo')
+rank, ws = dist.get_rank(), dist.get_world_size()
+hist = fit_problem(rank, ws, dist.group.WORLD)
+print(json.dumps({'rank': rank, 'loss': hist['loss'], 'W': torch.view_as_real(hist['W']).flatten().tolist()}))
+'''
+
+
+def fit_problem(rank, ws, group):
+    """Two Adam steps of the channel fit on four n=4 circuits, this rank's
+    share of them (i % ws == rank), marginals from the oracle (differentiable
+    in the channel tensor); the gradient and loss summed over ``group``."""
+    import torch
+    from oracle import channel_fit as C, mpdo_oracle as O
+    from mpdo_gb300 import channel_fit as F
+    circs = [C.random_circuit(4, 3, s) for s in range(4)]
+    data = torch.stack([C.marginals(a, C.kraus(C.hidden_isometry(7, 0.05)), 16, 4) for a in circs])
+    mine = [i for i in range(len(circs)) if i % ws == rank]
+
+    class OracleFitter:
+        def marginals(self, t):
+            out = []
+            for i in mine:
+                st = O.product_state([[1, 0]] * 4, connected=True)
+                O.evolve(st, C.circuit_ops(circs[i], t), chi=16, kappa=4, noisy=True)
+                out.append(torch.stack([O.expect_ops(st, {q: C._Z}) for q in range(4)]))
+            return torch.stack(out)
+    return F.fit(OracleFitter(), data[mine], steps=2, group=group)
+
+
+@pytest.mark.timeout(900)
+def test_channel_fit_gradient_allreduce():
+    # config 4 over two ranks: each evolves half of the circuits, the 16 x 4
+    # complex gradient is summed once per Adam step, and both ranks end on
+    # the W that one process fitting all circuits reaches
+    import torch
+    outs = _launch(['-c', _FIT_CODE], _free_port())
+    for rc, _, err in outs:
+        assert rc == 0, err[-2000:]
+    got = [json.loads(o[1].strip().splitlines()[-1]) for o in outs]
+    ref = fit_problem(0, 1, None)
+    w_ref = torch.view_as_real(ref['W']).flatten()
+    for g in got:
+        assert max(abs(a - b) for a, b in zip(g['loss'], ref['loss'])) < 1e-12 * max(ref['loss'])
+        # Adam's early steps are about lr * g / |g| per entry, so entries whose
+        # gradient is near zero turn the summation order's rounding into
+        # differences far above 1e-16; 1e-6 is 1/20000 of one step (lr 0.02)
+        assert (torch.tensor(g['W']) - w_ref).abs().max() < 1e-6

@@ -159,12 +159,24 @@ class _Marginals(torch.autograd.Function):
         return None, torch.from_numpy(g).to(dtype=ctx.dtype, device=ctx.device)
 
 
+def _allreduce_sum(x: torch.Tensor, group) -> torch.Tensor:
+    import torch.distributed as dist
+    r = torch.view_as_real(x) if x.is_complex() else x
+    dist.all_reduce(r, op=dist.ReduceOp.SUM, group=group)
+    return x
+
+
 def fit(fitter: Fitter, data: torch.Tensor, steps: int, lr: float = 0.02, K_true: Optional[torch.Tensor] = None,
-        init_seed: int = 1, init_eps: float = 1e-2, callback=None):
+        init_seed: int = 1, init_eps: float = 1e-2, callback=None, group=None):
     """Adam on W (16 x 4 complex) minimising sum_c ||<Z>_c - data_c||^2,
     starting from the identity channel moved by ``init_eps`` (the exact
     identity is stationary for every dissipative direction).  Returns the
-    loss per step (before the update) and, with ``K_true``, the proxy."""
+    loss per step (before the update) and, with ``K_true``, the proxy.
+
+    Over several GPUs each rank passes a ``fitter`` over its own circuits
+    (and their ``data`` rows) and a process ``group``: the loss and the
+    gradient of W (64 complex numbers) are summed over the group once per
+    step, so every rank takes the same Adam step from the same W."""
     W = hidden_isometry(seed=init_seed, eps=init_eps).clone().requires_grad_(True)
     opt = torch.optim.Adam([W], lr=lr)
     hist = {'loss': [], 'proxy': []}
@@ -174,6 +186,9 @@ def fit(fitter: Fitter, data: torch.Tensor, steps: int, lr: float = 0.02, K_true
         m = fitter.marginals(cz_channel_tensor(K))
         loss = ((m - data) ** 2).sum()
         loss.backward()
+        if group is not None:
+            _allreduce_sum(W.grad, group)
+            loss = _allreduce_sum(loss.detach().clone(), group)
         hist['loss'].append(float(loss.detach()))
         if K_true is not None:
             hist['proxy'].append(diamond_proxy(K, K_true))
