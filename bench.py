@@ -703,6 +703,8 @@ def uneven_arm(args):
     all_layers = allreduce_sum(layers, ws)
     all_gates = allreduce_sum(gates, ws)
     value = all_layers * args.steps / (total_ms / 1e3)
+    print(f'uneven batch: {total_ms / args.steps / 1e3:.1f} s per step, {value:.1f} gate-layers/s', file=sys.stderr,
+          flush=True)
     seq = None
     if args.sequential:
         eng = Engine.get(local)
@@ -714,6 +716,8 @@ def uneven_arm(args):
             eng.sync()
             t_seq.append(time.perf_counter() - t0)
             del ch
+            print(f'sequential: {w.name}: {t_seq[-1]:.2f} s ({len(t_seq)}/{len(works)}, {sum(t_seq):.1f} s so far)',
+                  file=sys.stderr, flush=True)
         seq_s = allreduce_max(sum(t_seq), ws)
         seq = {'value': all_layers / seq_s, 'unit': 'gate-layers/s', 'seconds': seq_s,
                'path': 'the same circuits one at a time through one engine (Chain ops), wall clock',

@@ -160,20 +160,50 @@ __global__ void __launch_bounds__(QR_NT) k_qr_factor(int m, int n, int mc, View<
     if (tid == 0) tau_out[(int64_t)c * n + j] = tau;
     const bool ident = tau.x == T(0) && tau.y == T(0);
     const cx<T> ctau = cconj<T>(tau), cscl = cconj<T>(scl);
-    for (int k = j + 1 + warp; k < n; k += nw) {
+    // two trailing columns per warp and pass (k, k + nw): one read of the
+    // reflector serves both, and their dot / reduce / update chains overlap;
+    // each column's arithmetic is the same as one at a time
+    for (int k = j + 1 + warp; k < n; k += 2 * nw) {
+      const int k2 = k + nw;
+      const bool two = k2 < n;
       cx<T> *Wk = W + k * ld;
+      cx<T> *Wk2 = W + (two ? k2 : k) * ld;
       if (!ident) {
-        cx<T> d = czero<T>();
-        if (!debris)
-          for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(d, W[j * ld + i], Wk[i]);
+        cx<T> d = czero<T>(), d2 = czero<T>();
+        if (!debris) {
+          if (two) {
+            for (int i = j + 1 + lane; i < rows; i += 32) {
+              const cx<T> v = W[j * ld + i];
+              cfmac<T>(d, v, Wk[i]);
+              cfmac<T>(d2, v, Wk2[i]);
+            }
+          } else {
+            for (int i = j + 1 + lane; i < rows; i += 32) cfmac<T>(d, W[j * ld + i], Wk[i]);
+          }
+        }
         d.x = warp_sum(d.x); d.y = warp_sum(d.y);
+        if (two) { d2.x = warp_sum(d2.x); d2.y = warp_sum(d2.y); }
         // w = tau^H (W[j][k] + v^H W[:, k]) with v = scl x
         const cx<T> w = cmul<T>(ctau, cadd<T>(Wk[j], cmul<T>(cscl, d)));
         const cx<T> g = cmul<T>(scl, w);
+        const cx<T> w2 = cmul<T>(ctau, cadd<T>(Wk2[j], cmul<T>(cscl, d2)));
+        const cx<T> g2 = cmul<T>(scl, w2);
         __syncwarp();
-        if (lane == 0) Wk[j] = csub<T>(Wk[j], w);
-        if (!debris)
-          for (int i = j + 1 + lane; i < rows; i += 32) Wk[i] = csub<T>(Wk[i], cmul<T>(W[j * ld + i], g));
+        if (lane == 0) {
+          Wk[j] = csub<T>(Wk[j], w);
+          if (two) Wk2[j] = csub<T>(Wk2[j], w2);
+        }
+        if (!debris) {
+          if (two) {
+            for (int i = j + 1 + lane; i < rows; i += 32) {
+              const cx<T> v = W[j * ld + i];
+              Wk[i] = csub<T>(Wk[i], cmul<T>(v, g));
+              Wk2[i] = csub<T>(Wk2[i], cmul<T>(v, g2));
+            }
+          } else {
+            for (int i = j + 1 + lane; i < rows; i += 32) Wk[i] = csub<T>(Wk[i], cmul<T>(W[j * ld + i], g));
+          }
+        }
       }
       if (k == j + 1 && k < kc) {
         __syncwarp();
