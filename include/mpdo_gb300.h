@@ -96,6 +96,12 @@ mpdo_status mpdo_engine_set_stream(mpdo_engine_t eng, void *stream);
  *   "bjacobi_bs" block width (columns per block) of the wide-bond block
  *                Jacobi, capped by shared memory; 0 (default) picks
  *                max(8, n / 16) up to 32.
+ *   "bjacobi_fused" 1 (default): the block Jacobi runs as one launch on a
+ *                thread-block cluster (one CTA per block pair, at most 16)
+ *                that stops on the device after the first sweep without a
+ *                rotation (at most 40 sweeps); 0, or where the cluster does
+ *                not fit: one launch per tournament round and a host read of
+ *                the rotation flag after every sweep.  Same columns either way.
  *   "tsqr_ratio" TSQR chunks hold at least this many times the column count
  *                in rows (shared memory when they fit, else global memory);
  *                default 3, so every level shrinks the stacked R threefold.

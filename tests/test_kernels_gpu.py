@@ -187,3 +187,41 @@ def test_split_wide_tridiagonal_matches_jacobi(eng, m, n, keep, decay, dtype, to
     np.testing.assert_allclose(L0 @ R0, best, atol=tol * s[0] * 10)
     g = L1.conj().T @ L1
     np.testing.assert_allclose(np.diag(g).real, s[:keep], atol=tol * s[0])
+
+
+@pytest.mark.parametrize('m,n,keep', [(128, 2048, 64), (256, 8192, 64), (200, 600, 100)])
+@pytest.mark.parametrize('dtype', ['complex64', 'complex128'])
+def test_block_jacobi_cluster_matches_rounds(eng, m, n, keep, dtype):
+    # The wide-bond block Jacobi runs as one thread-block-cluster launch that
+    # decides convergence on the device, or as one launch per tournament round
+    # with the host reading the rotation flag after each sweep.  Same rounds,
+    # same per-round arithmetic: the splits must agree to rounding (they are
+    # expected to be identical).  m=128 and 256 use 8-CTA clusters; m=200 has
+    # 17 blocks, a 9-CTA cluster, which a device may refuse (the engine then
+    # takes the per-round launches, so only the results are compared there).
+    y = _rand(m, n, 5 * m + n)
+    out, launches = {}, {}
+    eng.set_option('wide_eig', 0)      # block Jacobi in complex128 too
+    eng.set_option('wide_range', 0)
+    try:
+        for fused in (0, 1):
+            eng.set_option('bjacobi_fused', fused)
+            eng.profile(True)
+            out[fused] = eng.debug_split(y, keep, dtype)
+            launches[fused] = eng.profile_read()['bjacobi']['launches']
+            eng.profile(False)
+    finally:
+        eng.set_option('bjacobi_fused', 1)
+        eng.set_option('wide_eig', -1)
+        eng.set_option('wide_range', -1)
+    (L0, R0), (L1, R1) = out[0], out[1]
+    scale = np.abs(L0 @ R0).max()
+    tol = 1e-12 if dtype == 'complex128' else 1e-6
+    np.testing.assert_allclose(L1 @ R1, L0 @ R0, atol=tol * scale)
+    np.testing.assert_allclose(np.abs(L1), np.abs(L0), atol=tol * np.abs(L0).max() * 10)
+    assert launches[0] > 8                  # several outer sweeps of 15 rounds
+    if m != 200:
+        assert launches[1] == 1
+    u, s, vh = np.linalg.svd(y, full_matrices=False)
+    best = (u[:, :keep] * s[:keep]) @ vh[:keep]
+    np.testing.assert_allclose(L1 @ R1, best, atol=(1e-10 if dtype == 'complex128' else 3e-5) * s[0] * 10)

@@ -187,7 +187,12 @@ void right_svd(Engine &e, int m, int n, const View<T> &in, DBuf<cx<T>> &W, DBuf<
 // --------------------------------------------------- wide-bond SVD ----
 // One-sided block Jacobi on the columns of X (m x n, column-major, in place):
 // tournament ordering over column blocks, one CTA per block pair per round,
-// repeated until an outer sweep makes no rotation.
+// repeated until an outer sweep makes no rotation (at most 40 sweeps).  By
+// default the whole iteration is one launch on a thread-block cluster that
+// decides convergence on the device; where the cluster does not fit (more
+// than 32 blocks, or the device refuses it) every round is its own launch and
+// the host reads the rotation flag after each sweep.  Both give the same
+// columns.
 template <typename T>
 static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
   const size_t esz = sizeof(cx<T>), cap = 200 * 1024;
@@ -201,6 +206,19 @@ static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
   const int nblk = (n + bs - 1) / bs;
   const int nb = nblk + (nblk & 1);
   const int rounds = nb - 1, np = nb / 2;
+  constexpr int kMaxOuter = 40;
+  DBuf<T> gmax(e, 1);
+  colmax2<T>(e.stream, m, n, X, gmax.p);
+  // algorithmic work: one thin SVD of the m x n matrix (4 (4 m n^2 + 22 n^3)),
+  // booked once; repeated sweeps add none
+  const double fl = 4.0 * (4.0 * m * (double)n * n + 22.0 * (double)n * n * n);
+  if (e.bjacobi_fused && bjacobi_cluster_fits<T>(m, n, bs)) {
+    cudaError_t err = cudaSuccess;
+    prof(e, K_BJACOBI, fl, (double)esz * m * n * 2, [&] {
+      err = bjacobi_cluster<T>(e.stream, m, n, bs, nblk, X, gmax.p, 2, kMaxOuter, nullptr);
+    });
+    if (err == cudaSuccess) return;
+  }
   std::vector<int> pairs((size_t)rounds * np * 2);
   for (int r = 0; r < rounds; ++r)
     for (int p = 0; p < np; ++p) {
@@ -211,17 +229,12 @@ static void block_jacobi(Engine &e, int m, int n, cx<T> *X) {
       pairs[((size_t)r * np + p) * 2 + 1] = c;
     }
   DBuf<int> dp(e, pairs.size()), flag(e, 1);
-  DBuf<T> gmax(e, 1);
   MPDO_CUDA_CHECK(cudaMemcpyAsync(dp.p, pairs.data(), pairs.size() * sizeof(int), cudaMemcpyHostToDevice, e.stream));
-  colmax2<T>(e.stream, m, n, X, gmax.p);
   int hflag = 1;
-  for (int outer = 0; outer < 40 && hflag; ++outer) {
+  for (int outer = 0; outer < kMaxOuter && hflag; ++outer) {
     MPDO_CUDA_CHECK(cudaMemsetAsync(flag.p, 0, sizeof(int), e.stream));
-    // algorithmic work: one thin SVD of the m x n matrix (4 (4 m n^2 + 22 n^3)),
-    // booked once on the first round; repeated sweeps add none
     for (int r = 0; r < rounds; ++r)
-      prof(e, K_BJACOBI, (outer == 0 && r == 0) ? 4.0 * (4.0 * m * (double)n * n + 22.0 * (double)n * n * n) : 0.0,
-           (double)esz * m * n * 2, [&] {
+      prof(e, K_BJACOBI, (outer == 0 && r == 0) ? fl : 0.0, (double)esz * m * n * 2, [&] {
         bjacobi_round<T>(e.stream, m, n, bs, nblk, X, dp.p + (size_t)r * np * 2, np, gmax.p, 2, flag.p);
       });
     MPDO_CUDA_CHECK(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
@@ -1635,6 +1648,7 @@ mpdo_status mpdo_engine_set_option(mpdo_engine_t eng, const char *name, double v
       need(value >= 0 && value <= 64, "bjacobi_bs out of range");
       e.bjacobi_bs = (int)value;
     }
+    else if (k == "bjacobi_fused") e.bjacobi_fused = value != 0;
     else if (k == "tsqr_ratio") {
       need(value >= 1.0 && value <= 64.0, "tsqr_ratio out of range");
       e.tsqr_ratio = value;

@@ -51,6 +51,7 @@ struct Engine {
   // (every level shrinks the stack by about that factor)
   double tsqr_ratio = 3.0;
   int bjacobi_bs = 0;               // block-Jacobi block width (columns); 0: from the shared-memory cap
+  bool bjacobi_fused = true;        // block Jacobi as one thread-block-cluster launch (else one launch per round)
   int first_status = 0;
   // per-kernel-class profiling (CUDA events around each launch)
   struct ProfRec { int cls; cudaEvent_t a, b; double flops, bytes; };

@@ -56,6 +56,16 @@ void jacobi_svd(cudaStream_t st, int batch, int m, int n, const View<T> &in, cx<
 template <typename T>
 void bjacobi_round(cudaStream_t st, int m, int n, int bs, int nblk, cx<T> *X, const int *pairs_round, int npairs,
                    const T *gmax2, int inner_sweeps, int *flag);
+// All outer sweeps of the same block Jacobi in one launch on a thread-block
+// cluster of ceil(nblk / 2) CTAs (at most 16), stopping after the first sweep
+// without a rotation or after max_outer sweeps; the per-round arithmetic is
+// bjacobi_round's.  Returns the launch status: an error means nothing ran (the
+// cluster does not fit this device or shape) and the caller uses the
+// per-round launches.  sweeps_out (nullable, device): outer sweeps run.
+template <typename T> bool bjacobi_cluster_fits(int m, int n, int bs);
+template <typename T>
+cudaError_t bjacobi_cluster(cudaStream_t st, int m, int n, int bs, int nblk, cx<T> *X, const T *gmax2,
+                            int inner_sweeps, int max_outer, int *sweeps_out);
 // *out = max_j |X[:, j]|^2 for an m x n column-major X
 template <typename T>
 void colmax2(cudaStream_t st, int m, int n, const cx<T> *X, T *out);

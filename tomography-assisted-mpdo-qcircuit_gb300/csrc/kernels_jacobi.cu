@@ -12,6 +12,12 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cooperative_groups.h>
+#include <mutex>
+#include <set>
+#include <tuple>
+
+namespace cg = cooperative_groups;
 
 namespace mpdo {
 
@@ -255,40 +261,38 @@ void jacobi_svd(cudaStream_t st, int batch, int m, int n, const View<T> &in, cx<
 
 namespace {
 // ------------------------------------------------------ block Jacobi -----
-// One tournament round of a one-sided block-Jacobi sweep over the columns of X
-// (m x n, column-major in global memory).  CTA p loads the column blocks
-// pairs[2p], pairs[2p+1] (bs columns each; an id >= nblk is an empty block)
-// into shared memory, orthogonalises them against each other with up to
-// inner_sweeps one-sided Jacobi sweeps (no vector accumulation), writes them
-// back, and sets *flag when it rotated anything.  gmax2: the largest squared
-// column norm, for the rounding-level floor.
+// a complex load that bypasses L1 (data another SM wrote since this SM last
+// read the line must come from L2)
+template <typename T> __device__ __forceinline__ cx<T> ldcg_cx(const cx<T> *p) { return __ldcg(p); }
+
+// The columns of X (m x n, column-major in global memory) are cut into blocks
+// of bs columns (nblk blocks; an id >= nblk is an empty block).  An outer
+// sweep visits every pair of blocks once in nb - 1 tournament rounds of nb / 2
+// disjoint pairs (nb = nblk rounded up to even).  Pair p of round r is
+// (a, c) = (nb - 1, r) for p = 0, else ((r + p) mod (nb - 1), (r - p) mod (nb - 1)).
+__device__ __forceinline__ void bj_pair_of(int nb, int r, int p, int &a, int &c) {
+  if (p == 0) { a = nb - 1; c = r; }
+  else { a = (r + p) % (nb - 1); c = (r - p + nb - 1) % (nb - 1); }
+}
+
+// Orthogonalises the two blocks held in shared memory S (columns [0, w0) of
+// the first block, [w0, w0 + w1) of the second; m rows, column-major) against
+// each other with up to inner_sweeps one-sided Jacobi sweeps (no vector
+// accumulation).  Every thread of the CTA calls it; the result (whether any
+// rotation happened) is the same in all threads.  nrm2 holds >= w0 + w1
+// entries of shared memory.
 template <typename T>
-__global__ void __launch_bounds__(512) k_bjacobi(int m, int n, int bs, int nblk, cx<T> *X, const int *pairs,
-                                                 T tol, const T *gmax2, int inner_sweeps, int *flag) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int rot_count, any_rot;
-  cx<T> *S = reinterpret_cast<cx<T> *>(smem_raw);
-  const int b0 = pairs[2 * blockIdx.x], b1 = pairs[2 * blockIdx.x + 1];
-  const int c0 = b0 * bs, c1 = b1 * bs;
-  const int w0 = (b0 < nblk) ? min(bs, n - c0) : 0;
-  const int w1 = (b1 < nblk) ? min(bs, n - c1) : 0;
+__device__ __forceinline__ bool bj_pair_sweeps(cx<T> *S, int m, int w0, int w1, T tol, T floor_abs,
+                                               int inner_sweeps, T *nrm2, int *rot_count) {
   const int nc = w0 + w1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  if (tid == 0) any_rot = 0;
-  for (int64_t idx = tid; idx < (int64_t)m * nc; idx += blockDim.x) {
-    const int i = (int)(idx % m), j = (int)(idx / m);
-    const int col = j < w0 ? c0 + j : c1 + (j - w0);
-    S[(int64_t)j * m + i] = X[(int64_t)col * m + i];
-  }
-  __syncthreads();
-  const T floor_abs = (*gmax2) * T(16) * T(n) * Eps<T>::v * Eps<T>::v;
   const int ne = nc + (nc & 1);
   const int npairs = ne / 2;
+  bool any = false;
   // squared column norms, recomputed at the start of every inner sweep and
   // carried through rotations exactly as the 2 x 2 Gram's diagonal moves
   // (alpha' = alpha - t|g|, beta' = beta + t|g|), so a pair costs one
   // reduction (its inner product) instead of three
-  __shared__ T nrm2[64];
   auto rotate_pair = [&](int pc, int qc) -> bool {
     const T al = nrm2[pc], be = nrm2[qc];
     T t, g, cs, sn;
@@ -306,7 +310,7 @@ __global__ void __launch_bounds__(512) k_bjacobi(int m, int n, int bs, int nblk,
   // two blocks are revisited: bs steps of bs disjoint pairs
   const bool cross_only_ok = (w0 == w1) && w0 > 0;
   for (int sw = 0; sw < inner_sweeps && nc >= 2; ++sw) {
-    if (tid == 0) rot_count = 0;
+    if (tid == 0) *rot_count = 0;
     for (int j = warp; j < nc; j += nw) {
       T sq = T(0);
       for (int i = lane; i < m; i += 32) sq += cabs2<T>(S[(int64_t)j * m + i]);
@@ -318,32 +322,126 @@ __global__ void __launch_bounds__(512) k_bjacobi(int m, int n, int bs, int nblk,
       for (int r = 0; r < ne - 1; ++r) {
         for (int p = warp; p < npairs; p += nw) {
           int a, c;
-          if (p == 0) { a = ne - 1; c = r; }
-          else { a = (r + p) % (ne - 1); c = (r - p + ne - 1) % (ne - 1); }
+          bj_pair_of(ne, r, p, a, c);
           if (a >= nc || c >= nc) continue;
-          if (rotate_pair(min(a, c), max(a, c)) && lane == 0) atomicAdd(&rot_count, 1);
+          if (rotate_pair(min(a, c), max(a, c)) && lane == 0) atomicAdd(rot_count, 1);
         }
         __syncthreads();
       }
     } else {
       for (int st = 0; st < w0; ++st) {
         for (int i = warp; i < w0; i += nw)
-          if (rotate_pair(i, w0 + (i + st) % w0) && lane == 0) atomicAdd(&rot_count, 1);
+          if (rotate_pair(i, w0 + (i + st) % w0) && lane == 0) atomicAdd(rot_count, 1);
         __syncthreads();
       }
     }
-    const int rc = rot_count;
+    const int rc = *rot_count;
     __syncthreads();
     if (rc == 0) break;
-    if (tid == 0) any_rot = 1;
+    any = true;
   }
   __syncthreads();
+  return any;
+}
+
+// One tournament round of a one-sided block-Jacobi sweep.  CTA p loads the
+// column blocks pairs[2p], pairs[2p+1] into shared memory, orthogonalises them
+// against each other (bj_pair_sweeps), writes them back, and sets *flag when
+// it rotated anything.  gmax2: the largest squared column norm, for the
+// rounding-level floor.
+template <typename T>
+__global__ void __launch_bounds__(512) k_bjacobi(int m, int n, int bs, int nblk, cx<T> *X, const int *pairs,
+                                                 T tol, const T *gmax2, int inner_sweeps, int *flag) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int rot_count;
+  __shared__ T nrm2[64];
+  cx<T> *S = reinterpret_cast<cx<T> *>(smem_raw);
+  const int b0 = pairs[2 * blockIdx.x], b1 = pairs[2 * blockIdx.x + 1];
+  const int c0 = b0 * bs, c1 = b1 * bs;
+  const int w0 = (b0 < nblk) ? min(bs, n - c0) : 0;
+  const int w1 = (b1 < nblk) ? min(bs, n - c1) : 0;
+  const int nc = w0 + w1;
+  const int tid = threadIdx.x;
+  for (int64_t idx = tid; idx < (int64_t)m * nc; idx += blockDim.x) {
+    const int i = (int)(idx % m), j = (int)(idx / m);
+    const int col = j < w0 ? c0 + j : c1 + (j - w0);
+    S[(int64_t)j * m + i] = X[(int64_t)col * m + i];
+  }
+  __syncthreads();
+  const T floor_abs = (*gmax2) * T(16) * T(n) * Eps<T>::v * Eps<T>::v;
+  const bool any_rot = bj_pair_sweeps<T>(S, m, w0, w1, tol, floor_abs, inner_sweeps, nrm2, &rot_count);
   for (int64_t idx = tid; idx < (int64_t)m * nc; idx += blockDim.x) {
     const int i = (int)(idx % m), j = (int)(idx / m);
     const int col = j < w0 ? c0 + j : c1 + (j - w0);
     X[(int64_t)col * m + i] = S[(int64_t)j * m + i];
   }
   if (tid == 0 && any_rot) atomicOr(flag, 1);
+}
+
+// The whole block-Jacobi iteration in one launch on one thread-block cluster
+// of nb / 2 CTAs: CTA p takes pair p of every round (bj_pair_of), loads its two
+// blocks from X, orthogonalises them and writes them back; a cluster barrier
+// separates the rounds (the blocks a CTA loads were written by other CTAs of
+// the cluster in the round before; loads bypass L1).  After each outer sweep
+// every CTA reads the rotation flags of all CTAs of the cluster (distributed
+// shared memory) and the cluster stops once a sweep rotated nothing, or after
+// max_outer sweeps.  The arithmetic per round is k_bjacobi's, in the same
+// order, so both paths give the same columns.  *sweeps_out (nullable): outer
+// sweeps run.
+template <typename T>
+__global__ void __launch_bounds__(512) k_bjacobi_cl(int m, int n, int bs, int nblk, cx<T> *X, T tol,
+                                                    const T *gmax2, int inner_sweeps, int max_outer,
+                                                    int *sweeps_out) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int p = (int)cl.block_rank();
+  const int np = (int)cl.num_blocks();
+  const int nb = 2 * np, rounds = nb - 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int rot_count;
+  __shared__ T nrm2[64];
+  // rotflag[s & 1]: this CTA rotated something in outer sweep s.  Cleared for
+  // sweep s + 1 after the first barrier of sweep s, when every CTA has read
+  // the flags of sweep s - 1 (same slot)
+  __shared__ int rotflag[2];
+  cx<T> *S = reinterpret_cast<cx<T> *>(smem_raw);
+  const int tid = threadIdx.x;
+  if (tid == 0) rotflag[0] = rotflag[1] = 0;
+  const T floor_abs = (*gmax2) * T(16) * T(n) * Eps<T>::v * Eps<T>::v;
+  cl.sync();
+  int outer = 0;
+  while (outer < max_outer) {
+    for (int r = 0; r < rounds; ++r) {
+      int b0, b1;
+      bj_pair_of(nb, r, p, b0, b1);
+      const int c0 = b0 * bs, c1 = b1 * bs;
+      const int w0 = (b0 < nblk) ? min(bs, n - c0) : 0;
+      const int w1 = (b1 < nblk) ? min(bs, n - c1) : 0;
+      const int nc = w0 + w1;
+      for (int64_t idx = tid; idx < (int64_t)m * nc; idx += blockDim.x) {
+        const int i = (int)(idx % m), j = (int)(idx / m);
+        const int col = j < w0 ? c0 + j : c1 + (j - w0);
+        S[(int64_t)j * m + i] = ldcg_cx<T>(X + (int64_t)col * m + i);
+      }
+      __syncthreads();
+      const bool any = bj_pair_sweeps<T>(S, m, w0, w1, tol, floor_abs, inner_sweeps, nrm2, &rot_count);
+      for (int64_t idx = tid; idx < (int64_t)m * nc; idx += blockDim.x) {
+        const int i = (int)(idx % m), j = (int)(idx / m);
+        const int col = j < w0 ? c0 + j : c1 + (j - w0);
+        X[(int64_t)col * m + i] = S[(int64_t)j * m + i];
+      }
+      if (tid == 0 && any) rotflag[outer & 1] = 1;
+      __threadfence();
+      cl.sync();
+      if (r == 0 && tid == 0) rotflag[(outer + 1) & 1] = 0;
+    }
+    int v = 0;
+    for (int q = 0; q < np; ++q) v |= *cl.map_shared_rank(&rotflag[outer & 1], q);
+    ++outer;
+    if (!v) break;
+  }
+  // no CTA leaves while another may still read its flags
+  cl.sync();
+  if (sweeps_out && p == 0 && tid == 0) *sweeps_out = outer;
 }
 
 template <typename T>
@@ -378,6 +476,81 @@ void bjacobi_round(cudaStream_t st, int m, int n, int bs, int nblk, cx<T> *X, co
 }
 
 template <typename T>
+bool bjacobi_cluster_fits(int m, int n, int bs) {
+  const int nblk = (n + bs - 1) / bs;
+  const int np = (nblk + (nblk & 1)) / 2;
+  return np >= 1 && np <= 16 && 2 * bs <= 64 && (size_t)m * 2 * bs * sizeof(cx<T>) <= SMEM_CAP;
+}
+
+template <typename T>
+cudaError_t bjacobi_cluster(cudaStream_t st, int m, int n, int bs, int nblk, cx<T> *X, const T *gmax2,
+                            int inner_sweeps, int max_outer, int *sweeps_out) {
+  const T tol = T(4) * sqrt(T(std::max(m, 1))) * Eps<T>::v;
+  const size_t bytes = (size_t)m * 2 * bs * sizeof(cx<T>);
+  const int np = (nblk + (nblk & 1)) / 2;
+  if (!bjacobi_cluster_fits<T>(m, n, bs)) return cudaErrorInvalidValue;
+  smem_optin(k_bjacobi_cl<T>);
+  // clusters above 8 CTAs need the non-portable opt-in, which CUDA keeps per
+  // device: set once per (kernel, device)
+  if (np > 8) {
+    static std::mutex mu;
+    static std::set<int> done;
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!done.count(dev)) {
+      err = cudaFuncSetAttribute(k_bjacobi_cl<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if (err != cudaSuccess) return err;
+      done.insert(dev);
+    }
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(np, 1, 1);
+  cfg.blockDim = dim3(512, 1, 1);
+  cfg.dynamicSmemBytes = bytes;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = np;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (np > 8) {
+    // a non-portable cluster must fit one GPC of this device: ask once per
+    // (device, cluster size, shared memory) and leave the per-round launches
+    // to the caller when it does not
+    static std::mutex mu;
+    static std::set<std::tuple<int, int, size_t>> ok, refused;
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    const auto key = std::make_tuple(dev, np, bytes);
+    std::lock_guard<std::mutex> lk(mu);
+    if (refused.count(key)) return cudaErrorInvalidClusterSize;
+    if (!ok.count(key)) {
+      int nclusters = 0;
+      err = cudaOccupancyMaxActiveClusters(&nclusters, k_bjacobi_cl<T>, &cfg);
+      if (err != cudaSuccess || nclusters < 1) {
+        cudaGetLastError();
+        refused.insert(key);
+        return cudaErrorInvalidClusterSize;
+      }
+      ok.insert(key);
+    }
+  }
+  cudaError_t err = cudaLaunchKernelEx(&cfg, k_bjacobi_cl<T>, m, n, bs, nblk, X, tol, gmax2, inner_sweeps, max_outer,
+                                       sweeps_out);
+  if (err != cudaSuccess) {
+    cudaGetLastError();          // not placed: the caller runs the per-round launches, nothing ran
+    return err;
+  }
+  count_launch();
+  return err;
+}
+
+template <typename T>
 void colmax2(cudaStream_t st, int m, int n, const cx<T> *X, T *out) {
   k_colmax2<T><<<1, 1024, 0, st>>>(m, n, X, out);
   count_launch();
@@ -387,6 +560,12 @@ template void bjacobi_round<float>(cudaStream_t, int, int, int, int, cx<float> *
                                    int, int *);
 template void bjacobi_round<double>(cudaStream_t, int, int, int, int, cx<double> *, const int *, int,
                                     const double *, int, int *);
+template bool bjacobi_cluster_fits<float>(int, int, int);
+template bool bjacobi_cluster_fits<double>(int, int, int);
+template cudaError_t bjacobi_cluster<float>(cudaStream_t, int, int, int, int, cx<float> *, const float *, int, int,
+                                            int *);
+template cudaError_t bjacobi_cluster<double>(cudaStream_t, int, int, int, int, cx<double> *, const double *, int,
+                                             int, int *);
 template void colmax2<float>(cudaStream_t, int, int, const cx<float> *, float *);
 template void colmax2<double>(cudaStream_t, int, int, const cx<double> *, double *);
 

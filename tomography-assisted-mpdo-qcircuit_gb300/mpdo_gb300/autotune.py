@@ -4,7 +4,10 @@ Only options that change nothing beyond rounding are tuned:
 
 * ``tsqr_ratio``  TSQR chunk rows per column (tree depth against chunk size);
 * ``bjacobi_bs``  block width of the wide-bond block Jacobi (CTAs per round
-                  against work per CTA; 0 = the built-in rule).
+                  against work per CTA; 0 = the built-in rule);
+* ``bjacobi_fused`` the wide-bond block Jacobi as one thread-block-cluster
+                  launch (1) or one launch per tournament round (0); both
+                  give the same columns.
 
 A workload class is (device name, precision, chi, kappa).  ``tune`` times a
 prefix of a representative circuit of the class (the n-qubit U3 + CZ/CNOT
@@ -23,8 +26,8 @@ import statistics
 import time
 from typing import Callable, Dict, Optional, Sequence
 
-DEFAULTS = {'tsqr_ratio': 3.0, 'bjacobi_bs': 0}
-CANDIDATES = {'tsqr_ratio': [2.0, 3.0, 4.0], 'bjacobi_bs': [0, 8, 12, 16, 24, 32]}
+DEFAULTS = {'tsqr_ratio': 3.0, 'bjacobi_bs': 0, 'bjacobi_fused': 1}
+CANDIDATES = {'tsqr_ratio': [2.0, 3.0, 4.0], 'bjacobi_bs': [0, 8, 12, 16, 24, 32], 'bjacobi_fused': [1, 0]}
 
 
 def cache_path() -> str:
