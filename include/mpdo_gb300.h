@@ -116,8 +116,9 @@ mpdo_status mpdo_engine_sync(mpdo_engine_t eng);
  * every launch is bracketed by CUDA events on the engine stream and its
  * algorithmic flop and byte counts are accumulated.  Classes: 0 GEMM,
  * 1 Householder QR factor, 2 QR explicit-Q apply, 3 one-sided Jacobi,
- * 4 Kraus 1q apply, 5 two-site gate mix, 6 other, 8 block-Jacobi rounds of
- * wide bonds (class 3 is the single-CTA Jacobi).  Class 7 returns counters
+ * 4 Kraus 1q apply, 5 two-site gate mix, 6 other, 8 block Jacobi of wide
+ * bonds (one launch per eigen-solve; one per round with bjacobi_fused = 0;
+ * class 3 is the single-CTA Jacobi).  Class 7 returns counters
  * instead: launches = wide bonds solved by the range finder, flops = wide
  * bonds solved by the exact block Jacobi, bytes = the largest accepted relative
  * residual |Y - Q Q^H Y|_F / |Y|_F, ms = wide bonds whose exact path used the
@@ -151,6 +152,21 @@ mpdo_status mpdo_chain_read_site(mpdo_chain_t ch, int site, double *host_out);
 /* Replace a site tensor from host (dims = {l, 2, a, r}). */
 mpdo_status mpdo_chain_write_site(mpdo_chain_t ch, int site, const int dims[4],
                                   const double *host_in);
+/* The same two copies with a caller's DEVICE buffer, so that a site crosses
+ * the boundary without a host round trip.  They replace the reads and writes
+ * of Node.tensor on the reference's state nodes (AbstractCircuit.py:115-116
+ * hands them out, Tools.py:44-72 names their legs), which hold torch tensors
+ * on the circuit's device.  The buffer holds l*2*a*r complex values in the
+ * chain's own precision, row-major [l][s][a][r]: interleaved floats for
+ * complex64 chains, interleaved doubles for complex128 chains.  It must be
+ * device or managed memory of the engine's device.  A host pointer or
+ * another device's memory is rejected with MPDO_ERR_INVALID.  The copy runs
+ * on the engine's stream.  The call returns once it has completed, so the
+ * caller may reuse its buffer at once.  Work on other streams that produces
+ * dev_in must be complete before the call. */
+mpdo_status mpdo_chain_read_site_device(mpdo_chain_t ch, int site, void *dev_out);
+mpdo_status mpdo_chain_write_site_device(mpdo_chain_t ch, int site, const int dims[4],
+                                         const void *dev_in);
 
 /* Gate (K = 1) or noisy gate (K Kraus operators) on one qubit.
  * kraus: [out][in][k] complex, 2*2*K entries.  The Kraus leg is flattened

@@ -43,7 +43,8 @@ class QubitNode:
     @property
     def tensor(self) -> Tensor:
         if self._chain is not None:
-            t = torch.as_tensor(self._chain.site(self._index))
+            # copied device to device from the engine's site buffer (no host copy)
+            t = self._chain.site_tensor(self._index)
             return t.to(dtype=self._dtype or t.dtype, device=self._device)
         return self._tensor
 

@@ -1502,6 +1502,43 @@ template <typename T> static void write_site(mpdo_chain_s *ch, int site, const i
   set_site<T>(ch, site, p, dims[0], dims[2], dims[3]);
 }
 
+// A caller's buffer for the device-memory site copies must be device (or
+// managed) memory that the engine's device can address.
+static void need_device_buffer(const Engine &e, const void *p) {
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    fail(MPDO_ERR_INVALID, "the site buffer is not device memory");
+  }
+  if (attr.type == cudaMemoryTypeManaged) return;
+  if (attr.type != cudaMemoryTypeDevice)
+    fail(MPDO_ERR_INVALID, "the site buffer is not device memory (host or unregistered pointer)");
+  if (attr.device != e.device)
+    fail(MPDO_ERR_INVALID, "the site buffer is on device " + std::to_string(attr.device) + ", the chain on device " +
+                               std::to_string(e.device));
+}
+
+template <typename T> static void read_site_device(mpdo_chain_s *ch, int site, void *out) {
+  Engine &e = ch->eng->e;
+  need_device_buffer(e, out);
+  materialize_touching<T>(ch, site);
+  const size_t n = ch->s[site].elems();
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(out, ch->s[site].p, n * sizeof(cx<T>), cudaMemcpyDeviceToDevice, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+}
+
+template <typename T>
+static void write_site_device(mpdo_chain_s *ch, int site, const int dims[4], const void *in) {
+  Engine &e = ch->eng->e;
+  need_device_buffer(e, in);
+  ch->pend1[site].on = false;                 // replaced by the written tensor
+  materialize_touching<T>(ch, site);
+  const size_t n = (size_t)dims[0] * 2 * dims[2] * dims[3];
+  cx<T> *p = static_cast<cx<T> *>(dalloc(e, n * sizeof(cx<T>)));
+  MPDO_CUDA_CHECK(cudaMemcpyAsync(p, in, n * sizeof(cx<T>), cudaMemcpyDeviceToDevice, e.stream));
+  MPDO_CUDA_CHECK(cudaStreamSynchronize(e.stream));
+  set_site<T>(ch, site, p, dims[0], dims[2], dims[3]);
+}
 
 // ------------------------------------------------------- test hooks -----
 template <typename T> static std::vector<cx<T>> to_cx(const double *h, size_t n) {
@@ -1822,6 +1859,25 @@ mpdo_status mpdo_chain_write_site(mpdo_chain_t ch, int site, const int dims[4], 
     need(dims[0] >= 1 && dims[1] == 2 && dims[2] >= 1 && dims[3] >= 1, "bad site dims");
     set_device(ch->eng);
     DISPATCH(ch, write_site, ch, site, dims, host_in);
+  });
+}
+
+mpdo_status mpdo_chain_read_site_device(mpdo_chain_t ch, int site, void *dev_out) {
+  return guard([&] {
+    need(ch && dev_out, "NULL argument");
+    need(site >= 0 && site < ch->n, "site out of range");
+    set_device(ch->eng);
+    DISPATCH(ch, read_site_device, ch, site, dev_out);
+  });
+}
+
+mpdo_status mpdo_chain_write_site_device(mpdo_chain_t ch, int site, const int dims[4], const void *dev_in) {
+  return guard([&] {
+    need(ch && dims && dev_in, "NULL argument");
+    need(site >= 0 && site < ch->n, "site out of range");
+    need(dims[0] >= 1 && dims[1] == 2 && dims[2] >= 1 && dims[3] >= 1, "bad site dims");
+    set_device(ch->eng);
+    DISPATCH(ch, write_site_device, ch, site, dims, dev_in);
   });
 }
 

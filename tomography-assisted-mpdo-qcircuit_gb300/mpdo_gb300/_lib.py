@@ -60,6 +60,8 @@ SIGNATURES = {
     'mpdo_chain_bond_present': (_I, [_P, _I, _IP]),
     'mpdo_chain_read_site': (_I, [_P, _I, _DP]),
     'mpdo_chain_write_site': (_I, [_P, _I, _IP, _DP]),
+    'mpdo_chain_read_site_device': (_I, [_P, _I, _P]),
+    'mpdo_chain_write_site_device': (_I, [_P, _I, _IP, _P]),
     'mpdo_apply_1q': (_I, [_P, _I, _DP, _I]),
     'mpdo_apply_2q': (_I, [_P, _I, _DP, _I, _D]),
     'mpdo_truncate': (_I, [_P, _I, _I, _D, _I, _DP]),

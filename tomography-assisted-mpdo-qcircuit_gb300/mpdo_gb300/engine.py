@@ -257,6 +257,31 @@ class Chain:
         buf = _cplx(t)
         check(self._lib.mpdo_chain_write_site(self.handle, int(i), d, _dptr(buf)))
 
+    def _torch_dtype(self):
+        import torch
+        return torch.complex64 if self.dtype == 'complex64' else torch.complex128
+
+    def site_tensor(self, i: int):
+        """Site i as a torch tensor (l, 2, a, r) on the engine's device, in the
+        chain's precision, copied device to device (``mpdo_chain_read_site_device``)."""
+        import torch
+        out = torch.empty(self.site_dims(i), dtype=self._torch_dtype(), device=f'cuda:{self.engine.device}')
+        check(self._lib.mpdo_chain_read_site_device(self.handle, int(i), C.c_void_p(out.data_ptr())))
+        return out
+
+    def write_site_tensor(self, i: int, tensor) -> None:
+        """Replace site i by a torch tensor (l, 2, a, r) without a host copy: it is
+        brought to the engine's device and the chain's precision, the work that
+        produced it is waited for, and it is copied device to device
+        (``mpdo_chain_write_site_device``)."""
+        import torch
+        t = tensor.to(device=f'cuda:{self.engine.device}', dtype=self._torch_dtype()).contiguous()
+        if t.dim() != 4 or t.shape[1] != 2:
+            raise ValueError(f'a site tensor has shape (l, 2, a, r), got {tuple(t.shape)}')
+        torch.cuda.current_stream(t.device).synchronize()
+        d = (C.c_int * 4)(*t.shape)
+        check(self._lib.mpdo_chain_write_site_device(self.handle, int(i), d, C.c_void_p(t.data_ptr())))
+
     # ---- readout ----------------------------------------------------------
     def reduced_dm(self, keep: Optional[Sequence[int]] = None) -> np.ndarray:
         keep = list(range(self.n)) if keep is None else sorted(int(q) for q in keep)
