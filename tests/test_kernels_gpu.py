@@ -1,5 +1,8 @@
 """Kernel-level GPU tests through the C-ABI test hooks: Householder QR (incl.
-TSQR levels) and QR + one-sided Jacobi SVD against numpy."""
+TSQR levels) and QR + one-sided Jacobi SVD against numpy.  The complex64
+tolerances sit 3-10x above the errors measured on a GB300 for these seeded
+inputs (QR 2.6e-7, right SVD 3.8e-6, split 1.3e-6, wide splits 4e-9 to
+3.2e-6, tridiagonal route 5.4e-7), on the scales each assertion states."""
 import numpy as np
 import pytest
 import torch
@@ -27,7 +30,7 @@ def _rand(m, n, seed, rank=None):
 
 
 @pytest.mark.parametrize('m,n', [(8, 8), (40, 13), (13, 40), (512, 64), (4096, 64), (33000, 32), (300, 150)])
-@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-11), ('complex64', 5e-5)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-11), ('complex64', 1e-6)])
 def test_qr(eng, m, n, dtype, tol):
     a = _rand(m, n, m + n)
     q, r = eng.debug_qr(a, dtype)
@@ -39,7 +42,7 @@ def test_qr(eng, m, n, dtype, tol):
 
 @pytest.mark.parametrize('m,n,rank', [(64, 64, None), (100, 20, None), (20, 100, None), (64, 64, 10), (256, 48, 5),
                                       (16, 3, 1)])
-@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 2e-5)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 1e-5)])
 def test_right_svd(eng, m, n, rank, dtype, tol):
     a = _rand(m, n, 7 * m + n, rank)
     w, s = eng.debug_svd(a, dtype)
@@ -58,7 +61,7 @@ def test_right_svd(eng, m, n, rank, dtype, tol):
 
 @pytest.mark.parametrize('m,n,keep,rank', [(8, 512, 8, None), (32, 1024, 8, None), (8, 1024, 8, 3), (64, 16, 8, None),
                                            (16, 4, 10, None), (256, 8192, 64, None), (4, 200, 6, None)])
-@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-5)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 5e-6)])
 def test_split(eng, m, n, keep, rank, dtype, tol):
     y = _rand(m, n, 3 * m + n, rank)
     L, R = eng.debug_split(y, keep, dtype)
@@ -73,7 +76,7 @@ def test_split(eng, m, n, keep, rank, dtype, tol):
         assert np.abs(L[:, k:]).max() == 0 and np.abs(R[k:]).max() == 0
 
 
-@pytest.mark.parametrize('dtype,scale,tol', [('complex128', 1e-160, 1e-11), ('complex64', 1e-21, 5e-5)])
+@pytest.mark.parametrize('dtype,scale,tol', [('complex128', 1e-160, 1e-11), ('complex64', 1e-21, 1e-6)])
 def test_qr_columns_near_underflow(eng, dtype, scale, tol):
     # rank-deficient factors carry junk directions whose squares underflow;
     # the reflectors must stay unitary (scaled norms)
@@ -89,7 +92,7 @@ def test_qr_columns_near_underflow(eng, dtype, scale, tol):
 
 
 @pytest.mark.parametrize('m,n,keep,rank', [(128, 2048, 128, 20), (256, 8192, 64, 40), (200, 300, 150, 7)])
-@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-5)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 1e-6)])
 def test_split_wide_rank_deficient(eng, m, n, keep, rank, dtype, tol):
     # wide bonds go through the Gram / block-Jacobi / Rayleigh-Ritz path; exact
     # rank deficiency must not break the orthonormality of the basis
@@ -110,7 +113,7 @@ def _decaying(m, n, seed, decades_per_sv):
 
 
 @pytest.mark.parametrize('decay,expect_range', [(0.25, True), (0.01, False)])
-@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-5)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 1e-5)])
 def test_split_wide_range_finder(eng, decay, expect_range, dtype, tol):
     # wide bonds first try the randomized range finder; it is accepted only when
     # the residual outside its span is at rounding level (fast-decaying
@@ -150,7 +153,7 @@ def test_split_wide_range_matches_exact(eng, dtype):
     np.testing.assert_allclose(L1 @ R1, L0 @ R0, atol=tol * np.abs(L0 @ R0).max() * 10)
 
 
-@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-5)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 1e-6)])
 def test_split_wide_512(eng, dtype, tol):
     # the pair bond at chi=128 (Mr = 512): Gram 512 x 512 through block Jacobi
     y = _decaying(512, 2048, 9, 0.02)
@@ -162,7 +165,7 @@ def test_split_wide_512(eng, dtype, tol):
 
 @pytest.mark.parametrize('m,n,keep,decay', [(128, 1024, 64, 0.03), (200, 1500, 80, 0.02), (256, 2048, 64, 0.01),
                                             (256, 4096, 64, 0.003), (512, 2048, 128, 0.01)])
-@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-4)])
+@pytest.mark.parametrize('dtype,tol', [('complex128', 1e-10), ('complex64', 3e-6)])
 def test_split_wide_tridiagonal_matches_jacobi(eng, m, n, keep, decay, dtype, tol):
     # the exact wide path diagonalises the Gram by cluster tridiagonalisation
     # (default) or block Jacobi; both must give the best rank-keep approximation
