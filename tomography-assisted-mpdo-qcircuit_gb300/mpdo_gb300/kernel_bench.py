@@ -88,47 +88,50 @@ def bjacobi(m: int = 256, ncols: int = 8192, keep: int = 64, reps: int = 5, batc
                   max_err=None, noisy=True, ops=o, z=True) for w, o in zip(works, ops)]
     bt = Batch.get(0, batch) if batch > 0 else None
     out, zs = [], {}
-    for fused in (1, 0):
-        eng.set_option('bjacobi_fused', fused)
-        eng.debug_split(y, keep, dtype)                       # warm-up
-        eng.sync()
-        eng.profile(True)
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            eng.debug_split(y, keep, dtype)
-        eng.sync()
-        split_s = (time.perf_counter() - t0) / reps
-        p = eng.profile_read()['bjacobi']
-        eng.profile(False)
-        rec = {'kernel': 'bjacobi', 'fused': fused, 'dtype': dtype, 'split': [m, ncols, keep],
-               'split_ms': 1e3 * split_s, 'split_bjacobi_launches': p['launches'] / reps,
-               'split_bjacobi_ms': p['ms'] / reps}
-        if not split_only:
-            evolve(0)                                         # warm-up
+    try:
+        for fused in (1, 0):
+            eng.set_option('bjacobi_fused', fused)
+            eng.debug_split(y, keep, dtype)                       # warm-up
+            eng.sync()
             eng.profile(True)
             t0 = time.perf_counter()
-            ch = evolve(0)
-            ev_s = time.perf_counter() - t0
-            pe = eng.profile_read()
+            for _ in range(reps):
+                eng.debug_split(y, keep, dtype)
+            eng.sync()
+            split_s = (time.perf_counter() - t0) / reps
+            p = eng.profile_read()['bjacobi']
             eng.profile(False)
-            del ch
-            rec.update(evolution_s=ev_s, evolution_bjacobi_launches=pe['bjacobi']['launches'],
-                       evolution_bjacobi_ms=pe['bjacobi']['ms'], evolution_wide_svd_ms=pe['phases']['wide_svd']['ms'])
+            rec = {'kernel': 'bjacobi', 'fused': fused, 'dtype': dtype, 'split': [m, ncols, keep],
+                   'split_ms': 1e3 * split_s, 'split_bjacobi_launches': p['launches'] / reps,
+                   'split_bjacobi_ms': p['ms'] / reps}
+            if not split_only:
+                evolve(0)                                         # warm-up
+                eng.profile(True)
+                t0 = time.perf_counter()
+                ch = evolve(0)
+                ev_s = time.perf_counter() - t0
+                pe = eng.profile_read()
+                eng.profile(False)
+                del ch
+                rec.update(evolution_s=ev_s, evolution_bjacobi_launches=pe['bjacobi']['launches'],
+                           evolution_bjacobi_ms=pe['bjacobi']['ms'], evolution_wide_svd_ms=pe['phases']['wide_svd']['ms'])
+            if bt is not None:
+                bt.set_option('bjacobi_fused', fused)
+                bt.run(progs)                                     # warm-up
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                res = bt.run(progs)
+                torch.cuda.synchronize()
+                bs_ = time.perf_counter() - t0
+                gates = sum(sum(1 for op in o if op[0] in ('1q', '2q')) for o in ops)
+                rec.update(batch=batch, batch_s=bs_, batch_gates_per_s=gates / bs_)
+                zs[fused] = np.concatenate([np.asarray(r['z']) for r in res])
+            out.append(rec)
+    finally:
+        eng.set_option('bjacobi_fused', 1)
         if bt is not None:
-            bt.set_option('bjacobi_fused', fused)
-            bt.run(progs)                                     # warm-up
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            res = bt.run(progs)
-            torch.cuda.synchronize()
-            bs_ = time.perf_counter() - t0
-            gates = sum(sum(1 for op in o if op[0] in ('1q', '2q')) for o in ops)
-            rec.update(batch=batch, batch_s=bs_, batch_gates_per_s=gates / bs_)
-            zs[fused] = np.concatenate([np.asarray(r['z']) for r in res])
-        out.append(rec)
-    eng.set_option('bjacobi_fused', 1)
+            bt.set_option('bjacobi_fused', 1)
     if bt is not None:
-        bt.set_option('bjacobi_fused', 1)
         out[-1]['batch_z_max_diff_between_modes'] = float(np.abs(zs[1] - zs[0]).max())
     return out
 
