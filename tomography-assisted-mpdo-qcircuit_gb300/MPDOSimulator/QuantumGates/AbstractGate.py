@@ -32,6 +32,7 @@ class Barrier(nn.Module):
 
 
 _MODULE_STATE = None
+_MODULE_FLAGS = None
 
 
 def _module_state() -> dict:
@@ -46,11 +47,12 @@ def _module_init(obj: nn.Module) -> None:
     parameter / buffer / submodule / hook containers on first access
     (``QuantumGate.__getattr__``).  A circuit builds one gate module per gate;
     a dozen fresh containers per gate made the cyclic garbage collector run
-    through the growing circuit over and over, half of the build time."""
-    d = obj.__dict__
-    for k, v in _module_state().items():
-        if not isinstance(v, (dict, set, list)):
-            d[k] = v
+    through the growing circuit over and over, half of the build time.  The
+    flags are picked out of nn.Module's state once per process."""
+    global _MODULE_FLAGS
+    if _MODULE_FLAGS is None:
+        _MODULE_FLAGS = {k: v for k, v in _module_state().items() if not isinstance(v, (dict, set, list))}
+    obj.__dict__.update(_MODULE_FLAGS)
 
 
 class QuantumGate(ABC, nn.Module):
@@ -58,9 +60,8 @@ class QuantumGate(ABC, nn.Module):
 
     def __init__(self, ideal: Optional[bool] = True, dtype=torch.complex64, device='cpu'):
         _module_init(self)
-        self.para = None
-        self._ideal = ideal
-        self.dtype, self.device = dtype, device
+        # plain attributes, set without the per-attribute module check
+        self.__dict__.update(para=None, _ideal=ideal, dtype=dtype, device=device)
 
     def __getattr__(self, name):
         # nn.Module's per-instance containers, created on first use (each
@@ -93,6 +94,9 @@ class QuantumGate(ABC, nn.Module):
         rdt = torch.float64 if self.dtype == torch.complex128 else torch.float32
 
         def conv(p):
+            tp = type(p)
+            if tp is float or tp is int:           # the common case first
+                return torch.tensor(float(p), dtype=rdt)
             if isinstance(p, Tensor):
                 return p.to(device=self.device, dtype=self.dtype if p.is_complex() else rdt)
             if isinstance(p, (float, int)):
